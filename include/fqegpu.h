@@ -1,0 +1,187 @@
+/*
+ * fqegpu — C ABI of the GB300 (sm_103a) implementation of the OpenFermion-FQE
+ * restricted H·psi path.  Plain pointers and sizes only; no CUDA or PyTorch
+ * types appear in a signature (streams are passed as `void*` holding a
+ * cudaStream_t, NULL = the legacy default stream).
+ *
+ * Memory conventions
+ *   - psi / sigma / dvec arrays are complex128, stored as interleaved
+ *     (re, im) doubles, C-order, alpha-major: coeff[a * lenb + b], exactly the
+ *     layout of FqeData.coeff (fqe_data.py:106).
+ *   - "d_" arguments are device pointers owned by the caller; "h_" arguments
+ *     are host pointers owned by the caller.  Integrals are always host arrays
+ *     in the reference's own layout (they are tiny and are prepared on the
+ *     host, as fqe_data.py:691-693 prepares them).
+ *   - Handles (graph, hamiltonian, workspace) own their device memory and are
+ *     released with the matching *_destroy call.
+ *
+ * Errors: every entry point returns an fqegpu_status; nothing exits, traps or
+ * prints.  The text of the last error of the calling thread is available from
+ * fqegpu_last_error().  The reference instead exits from safe_malloc
+ * (lib/macros.c:25-46) and returns void from its kernels.
+ */
+#ifndef FQEGPU_H
+#define FQEGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  FQEGPU_OK = 0,
+  FQEGPU_ERR_INVALID = 1,     /* bad shape / argument (reference: ValueError) */
+  FQEGPU_ERR_NOMEM = 2,       /* device or host allocation failed            */
+  FQEGPU_ERR_CUDA = 3,        /* CUDA runtime error (text in last_error)     */
+  FQEGPU_ERR_UNSUPPORTED = 4, /* valid request this build does not handle    */
+  FQEGPU_ERR_TIMEOUT = 5,     /* a bounded device wait gave up               */
+  FQEGPU_ERR_NUMERIC = 6,     /* non-finite value or series did not converge */
+} fqegpu_status;
+
+/* Contraction arithmetic of fqegpu_apply / fqegpu_taylor. */
+typedef enum {
+  FQEGPU_PREC_FP64 = 0,   /* plain FP64: the drop-in, matches the reference  */
+  FQEGPU_PREC_OZAKI = 1,  /* FP64 operands split into BF16 slices on the
+                             tcgen05 tensor cores, FP32 accumulation,
+                             compensated recombination (real integrals) */
+} fqegpu_precision;
+
+typedef struct fqegpu_graph_s *fqegpu_graph;
+typedef struct fqegpu_ham_s *fqegpu_ham;
+
+/* ---- library ------------------------------------------------------------ */
+int fqegpu_version(void);
+/* Copies the last error text of the calling thread (NUL terminated). */
+int fqegpu_last_error(char *buf, int buflen);
+/* Blocks until all work on `stream` is done; reports asynchronous errors. */
+int fqegpu_sync(void *stream);
+
+/* ---- K1: string graph ---------------------------------------------------
+ * Replaces FciGraph.__init__ (fci_graph.py:108-154) and the natives it calls:
+ * lexicographic_bitstring_generator (lib/bitstring.c:29-45),
+ * calculate_Z_matrix (lib/fci_graph.c:27-54), calculate_string_address
+ * (lib/fci_graph.c:136-147), build_mapping_strings (lib/fci_graph.c:76-121)
+ * and map_deexc (lib/fci_graph.c:57-73).  All tables are built on the device.
+ * norb <= 63, 0 <= nalpha, nbeta <= norb (fci_graph.py:124-137 checks). */
+int fqegpu_graph_create(int norb, int nalpha, int nbeta, void *stream,
+                        fqegpu_graph *out);
+int fqegpu_graph_destroy(fqegpu_graph g);
+/* lena, lenb, ndexca = nalpha*(norb-nalpha+1), ndexcb. */
+int fqegpu_graph_dims(fqegpu_graph g, int64_t *lena, int64_t *lenb,
+                      int *ndexca, int *ndexcb);
+/* Copy-outs of the device tables in the reference's formats (spin 0 = alpha,
+ * 1 = beta): strings uint64[len] (FciGraph._astr), Z int32[nele][norb]
+ * (_get_Z_matrix), dexc int32[len][ndexc][3] (FciGraph._dexca),
+ * map lengths int32[norb][norb] and maps int32[sum lengths][3], the
+ * concatenation in (i, j) i-major order of FciGraph._alpha_map[(i, j)]. */
+int fqegpu_graph_strings(fqegpu_graph g, int spin, uint64_t *h_out);
+int fqegpu_graph_zmatrix(fqegpu_graph g, int spin, int32_t *h_out);
+int fqegpu_graph_dexc(fqegpu_graph g, int spin, int32_t *h_out);
+int fqegpu_graph_map_lengths(fqegpu_graph g, int spin, int32_t *h_out);
+int fqegpu_graph_maps(fqegpu_graph g, int spin, int32_t *h_out);
+
+/* ---- restricted Hamiltonian ----------------------------------------------
+ * Prepares (h1, h2) of a RestrictedHamiltonian (restricted_hamiltonian.py)
+ * for one sector: h1' = h1 - sum_k h2'[i,k,k,j], h2'[i,k,j,l] = -h2[i,j,k,l]
+ * (fqe_data.py:691-693), with the one-body part folded into the pair matrix as
+ * h1'[ij] delta_kl / N_e.  h_h1: complex128 [norb][norb] (may be NULL),
+ * h_h2: complex128 [norb]^4 (may be NULL: one-body operator, the
+ * _apply_array_spatial1 case, fqe_data.py:477-531).  The pair space is
+ * compressed to norb(norb+1)/2 when the tensors have the real-orbital pair
+ * symmetries, as fqe_data.py:658-681 does for real integrals. */
+int fqegpu_ham_create(fqegpu_graph g, const double *h_h1, const double *h_h2,
+                      void *stream, fqegpu_ham *out);
+int fqegpu_ham_destroy(fqegpu_ham h);
+/* info[0] = pair count P, info[1] = 1 if compressed, info[2] = 1 if the
+ * integrals are a complex scalar times a real tensor, info[3] = scratch bytes
+ * of one apply at the current block width. */
+int fqegpu_ham_info(fqegpu_ham h, int64_t *info4);
+/* Upper bound on device scratch one apply may hold (default: 40% of free
+ * memory at creation).  Smaller budgets stream narrower beta-column blocks. */
+int fqegpu_ham_set_scratch_limit(fqegpu_ham h, int64_t bytes);
+
+/* Per-stage device time of the last apply on this handle (milliseconds,
+ * summed over beta-column blocks): [0] gather (K2), [1] pair contraction
+ * (K3), [2] scatter (K4).  Timing is measured with CUDA events recorded on
+ * the launching stream when enabled with fqegpu_ham_set_timing (off by
+ * default); fqegpu_ham_stage_ms waits for the last event.  No counterpart in
+ * the reference (its profiling is cProfile, profiling/profile_H_ring.py). */
+int fqegpu_ham_set_timing(fqegpu_ham h, int enable);
+int fqegpu_ham_stage_ms(fqegpu_ham h, double *h_ms3);
+
+/* ---- A2-A6: H·psi ---------------------------------------------------------
+ * d_sigma = alpha * (H d_psi) + beta * d_psi for the sector of the graph the
+ * Hamiltonian was created on.  Replaces, for one sector, FqeData.apply_inplace
+ * (fqe_data.py:421-475) with its three native calls
+ * lm_apply_array12_same_spin_opt x2 and lm_apply_array12_diff_spin_opt
+ * (lib/fqe_data.c:668-720, :973-996; Cython wrappers _fqe_data.pyx:609-765),
+ * and for one-body operators lm_apply_array1 (lib/fqe_data.c:272-302).
+ * Wavefunction._apply_array's e_0 term (wavefunction.py:396-397) is beta.
+ * d_psi and d_sigma must not alias. */
+int fqegpu_apply(fqegpu_ham h, const double *d_psi, double *d_sigma,
+                 double alpha_re, double alpha_im, double beta_re,
+                 double beta_im, int precision, void *stream);
+/* Same with host buffers: copies psi in and sigma out (pageable or pinned),
+ * synchronous.  This is the call a ctypes binding inside the reference's
+ * FqeData would make. */
+int fqegpu_apply_host(fqegpu_ham h, const double *h_psi, double *h_sigma,
+                      double alpha_re, double alpha_im, double beta_re,
+                      double beta_im, int precision);
+
+/* ---- A7: dvec ------------------------------------------------------------
+ * d_dvec[i][j][a][b] = sum_J <I|E_ij|J> psi_J   (zdvec_make,
+ * lib/fqe_data.c:350-377, FqeData.calculate_dvec_spatial fqe_data.py:2149)
+ * and its inverse scatter d_out[I] (+)= sum_ij sum_J <I|E_ij|J> dvec_ij[J]
+ * (zcoeff_make, lib/fqe_data.c:379-406, fqe_data.py:2309-2334). */
+int fqegpu_make_dvec(fqegpu_graph g, const double *d_psi, double *d_dvec,
+                     void *stream);
+int fqegpu_make_coeff(fqegpu_graph g, const double *d_dvec, double *d_out,
+                      int accumulate, void *stream);
+
+/* ---- A11: diagonal Coulomb -------------------------------------------------
+ * mode 0: d_psi[I] *= exp(E(I)) (zdiagonal_coulomb, lib/fqe_data.c:526-602)
+ * mode 1: d_psi[I] *= E(I)      (zdiagonal_coulomb_apply, :455-524)
+ * with E(I) = sum_{i in a} f_i + sum_{i,j in a} V_ij (same for b) plus the
+ * cross term (2 V_ij rows for mode 0 as the reference, V_ij + V_ji for
+ * mode 1).  h_diag complex128[norb], h_vij complex128[norb][norb], already
+ * multiplied by -i t for evolution (diagonal_coulomb.py:109-123). */
+int fqegpu_diagonal_coulomb(fqegpu_graph g, const double *h_diag,
+                            const double *h_vij, double *d_psi, int mode,
+                            void *stream);
+
+/* ---- A13: vector operations on complex128 arrays of n elements ----------
+ * FqeData.ax_plus_y / scale / norm (fqe_data.py:2620-2751), util.vdot
+ * (util.py:506-530).  Results of reductions go to host memory (the call
+ * synchronises on `stream`).  Reductions are deterministic. */
+int fqegpu_axpy(int64_t n, double a_re, double a_im, const double *d_x,
+                double *d_y, void *stream);
+int fqegpu_scale(int64_t n, double a_re, double a_im, double *d_x,
+                 void *stream);
+int fqegpu_vdot(int64_t n, const double *d_x, const double *d_y,
+                double *h_result2, void *stream);
+int fqegpu_norm2(int64_t n, const double *d_x, double *h_result,
+                 void *stream);
+
+/* ---- A10: Taylor propagator ------------------------------------------------
+ * d_psi <- sum_k (-i t H)^k / k! d_psi until ||term|| < accuracy, at most
+ * `expansion`-1 orders, then the e_0 phase exp(-i t e_0) (e0 passed in).
+ * Wavefunction.apply_generated_unitary 'taylor' (wavefunction.py:553-568,
+ * 605-606) and time_evolve's two-body branch (wavefunction.py:1042-1045).
+ * *h_terms receives the number of applies.  FQEGPU_ERR_NUMERIC if the series
+ * does not reach the accuracy (the reference raises RuntimeError). */
+int fqegpu_taylor(fqegpu_ham h, double *d_psi, double time, double e0_re,
+                  double e0_im, double accuracy, int expansion, int precision,
+                  int *h_terms, void *stream);
+
+/* ---- A12: Davidson support -----------------------------------------------
+ * d_diag[I] = <I|H|I> (real part, float64 [lena][lenb]) by the Slater-Condon
+ * rules, in one pass (the reference builds it with one expectationValue per
+ * determinant, algorithm/davidson.py:159-180). */
+int fqegpu_diagonal(fqegpu_ham h, double *d_diag, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FQEGPU_H */

@@ -1,0 +1,205 @@
+// Library plumbing (error text, version, sync) and the complex128 vector
+// operations of FqeData / util (A13): ax_plus_y, scale, norm, vdot.
+//
+// Reductions are two-pass with a fixed grid and a fixed summation tree, so a
+// result does not depend on scheduling (bit-reproducible run to run).
+#include <cstdarg>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace fqegpu {
+
+static thread_local char g_err[1024] = {0};
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+void clear_error() { g_err[0] = 0; }
+
+constexpr int kRedBlocks = 1024;
+constexpr int kRedThreads = 256;
+
+__global__ void k_axpy(int64_t n, double2 a, const double2* __restrict__ x,
+                       double2* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 xv = x[i];
+    double2 yv = y[i];
+    yv.x += a.x * xv.x - a.y * xv.y;
+    yv.y += a.x * xv.y + a.y * xv.x;
+    y[i] = yv;
+  }
+}
+
+__global__ void k_scale(int64_t n, double2 a, double2* __restrict__ x) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = x[i];
+    x[i] = make_double2(a.x * v.x - a.y * v.y, a.x * v.y + a.y * v.x);
+  }
+}
+
+// partial[b] = sum over this block's grid-stride share of conj(x) * y
+// (or |x|^2 when y == nullptr).
+__global__ void k_dot_partial(int64_t n, const double2* __restrict__ x,
+                              const double2* __restrict__ y,
+                              double2* __restrict__ partial) {
+  __shared__ double2 sh[kRedThreads];
+  double re = 0.0, im = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 a = x[i];
+    if (y) {
+      const double2 b = y[i];
+      re += a.x * b.x + a.y * b.y;
+      im += a.x * b.y - a.y * b.x;
+    } else {
+      re += a.x * a.x + a.y * a.y;
+    }
+  }
+  sh[threadIdx.x] = make_double2(re, im);
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sh[threadIdx.x].x += sh[threadIdx.x + s].x;
+      sh[threadIdx.x].y += sh[threadIdx.x + s].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void k_dot_final(int nparts, const double2* __restrict__ partial,
+                            double2* __restrict__ out) {
+  __shared__ double2 sh[kRedThreads];
+  double re = 0.0, im = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+    re += partial[i].x;
+    im += partial[i].y;
+  }
+  sh[threadIdx.x] = make_double2(re, im);
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sh[threadIdx.x].x += sh[threadIdx.x + s].x;
+      sh[threadIdx.x].y += sh[threadIdx.x + s].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+static int grid_for(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  const int64_t cap = (int64_t)kNumSMs * 16;
+  if (b > cap) b = cap;
+  return (int)(b > 0 ? b : 1);
+}
+
+int axpy_async(int64_t n, double2 a, const double2* x, double2* y,
+               cudaStream_t st) {
+  if (n <= 0) return FQEGPU_OK;
+  k_axpy<<<grid_for(n, 256), 256, 0, st>>>(n, a, x, y);
+  FQE_CUDA(cudaGetLastError());
+  return FQEGPU_OK;
+}
+
+int scale_async(int64_t n, double2 a, double2* x, cudaStream_t st) {
+  if (n <= 0) return FQEGPU_OK;
+  k_scale<<<grid_for(n, 256), 256, 0, st>>>(n, a, x);
+  FQE_CUDA(cudaGetLastError());
+  return FQEGPU_OK;
+}
+
+// Device-side dot into d_out (a double2 of device memory); scratch must hold
+// kRedBlocks double2.
+int dot_async(int64_t n, const double2* x, const double2* y, double2* scratch,
+              double2* d_out, cudaStream_t st) {
+  k_dot_partial<<<kRedBlocks, kRedThreads, 0, st>>>(n, x, y, scratch);
+  FQE_CUDA(cudaGetLastError());
+  k_dot_final<<<1, kRedThreads, 0, st>>>(kRedBlocks, scratch, d_out);
+  FQE_CUDA(cudaGetLastError());
+  return FQEGPU_OK;
+}
+
+int dot_scratch_bytes() { return (kRedBlocks + 1) * (int)sizeof(double2); }
+
+static int dot_host(int64_t n, const double2* x, const double2* y, double2* h,
+                    cudaStream_t st) {
+  double2* scratch = nullptr;
+  FQE_CUDA(cudaMallocAsync(&scratch, dot_scratch_bytes(), st));
+  int s = dot_async(n, x, y, scratch, scratch + kRedBlocks, st);
+  if (s == FQEGPU_OK) {
+    cudaError_t e = cudaMemcpyAsync(h, scratch + kRedBlocks, sizeof(double2),
+                                    cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      set_error("dot: %s", cudaGetErrorString(e));
+      s = FQEGPU_ERR_CUDA;
+    }
+  }
+  cudaFreeAsync(scratch, st);
+  return s;
+}
+
+}  // namespace fqegpu
+
+using namespace fqegpu;
+
+extern "C" int fqegpu_version(void) { return 100; }
+
+extern "C" int fqegpu_last_error(char* buf, int buflen) {
+  if (!buf || buflen <= 0) return FQEGPU_ERR_INVALID;
+  strncpy(buf, g_err, (size_t)buflen - 1);
+  buf[buflen - 1] = 0;
+  return FQEGPU_OK;
+}
+
+extern "C" int fqegpu_sync(void* stream) {
+  clear_error();
+  FQE_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  return FQEGPU_OK;
+}
+
+extern "C" int fqegpu_axpy(int64_t n, double a_re, double a_im, const double* d_x,
+                           double* d_y, void* stream) {
+  clear_error();
+  FQE_CHECK_ARG(n >= 0 && (n == 0 || (d_x && d_y)), "bad axpy arguments");
+  return axpy_async(n, make_double2(a_re, a_im), (const double2*)d_x,
+                    (double2*)d_y, (cudaStream_t)stream);
+}
+
+extern "C" int fqegpu_scale(int64_t n, double a_re, double a_im, double* d_x,
+                            void* stream) {
+  clear_error();
+  FQE_CHECK_ARG(n >= 0 && (n == 0 || d_x), "bad scale arguments");
+  return scale_async(n, make_double2(a_re, a_im), (double2*)d_x,
+                     (cudaStream_t)stream);
+}
+
+extern "C" int fqegpu_vdot(int64_t n, const double* d_x, const double* d_y,
+                           double* h_result2, void* stream) {
+  clear_error();
+  FQE_CHECK_ARG(n >= 0 && d_x && d_y && h_result2, "bad vdot arguments");
+  double2 r;
+  FQE_TRY(dot_host(n, (const double2*)d_x, (const double2*)d_y, &r,
+                   (cudaStream_t)stream));
+  h_result2[0] = r.x;
+  h_result2[1] = r.y;
+  return FQEGPU_OK;
+}
+
+extern "C" int fqegpu_norm2(int64_t n, const double* d_x, double* h_result,
+                            void* stream) {
+  clear_error();
+  FQE_CHECK_ARG(n >= 0 && d_x && h_result, "bad norm arguments");
+  double2 r;
+  FQE_TRY(dot_host(n, (const double2*)d_x, nullptr, &r, (cudaStream_t)stream));
+  *h_result = sqrt(r.x);
+  return FQEGPU_OK;
+}

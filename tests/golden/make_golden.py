@@ -1,0 +1,185 @@
+"""Generate tests/golden/*.npz by running the reference FQE (0.3.0).
+
+Run in a container where the reference sources are mounted and
+``make -C oracle ref`` has built its natives:
+
+    python tests/golden/make_golden.py
+
+Every fixture records the reference's own output for seeded inputs; the GPU
+tests and the oracle pin tests compare against these files, so nothing at test
+time needs the reference.  Inputs come from fqe_gb300.synthetic (a numpy-only
+module) or from numpy.random.default_rng with the seeds written below.
+"""
+
+import math
+import os
+import sys
+
+import numpy
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+sys.path.insert(0, os.path.join(REPO, "openfermion-fqe_gb300"))
+
+import ref_fqe  # noqa: E402
+from fqe_gb300 import synthetic  # noqa: E402  (numpy only)
+
+fqe = ref_fqe.import_fqe()
+from fqe.fqe_data import FqeData  # noqa: E402
+from fqe.fci_graph import FciGraph  # noqa: E402
+
+GRAPH_CASES = [(4, 2, 2), (6, 3, 2), (8, 4, 4), (5, 0, 3), (3, 3, 1),
+               (7, 2, 5), (1, 1, 0), (10, 5, 4)]
+APPLY_CASES = [  # (norb, nalpha, nbeta, kind, seed)
+    (4, 2, 2, "real", 1),
+    (6, 3, 2, "real", 2),
+    (8, 4, 4, "real", 0),
+    (5, 2, 3, "complex", 3),
+    (6, 1, 4, "nonsym", 4),
+    (7, 3, 3, "real", 5),
+    (4, 0, 2, "real", 6),
+    (6, 3, 3, "onebody", 7),
+    (5, 2, 2, "onebody_complex", 8),
+]
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name + ".npz")
+    numpy.savez_compressed(path, **arrays)
+    print("wrote", path, sum(a.nbytes for a in arrays.values()), "bytes raw")
+
+
+def graph_fixture():
+    out = {}
+    for norb, na, nb in GRAPH_CASES:
+        g = FciGraph(na, nb, norb)
+        tag = f"{norb}_{na}_{nb}"
+        out[f"astr_{tag}"] = numpy.asarray(g._astr, dtype=numpy.uint64)
+        out[f"bstr_{tag}"] = numpy.asarray(g._bstr, dtype=numpy.uint64)
+        out[f"dexca_{tag}"] = numpy.asarray(g._dexca, dtype=numpy.int32)
+        out[f"dexcb_{tag}"] = numpy.asarray(g._dexcb, dtype=numpy.int32)
+        maps = [numpy.asarray(g._alpha_map[(i, j)], dtype=numpy.int32).reshape(-1, 3)
+                for i in range(norb) for j in range(norb)]
+        out[f"amaplen_{tag}"] = numpy.array([len(m) for m in maps], dtype=numpy.int32)
+        out[f"amaps_{tag}"] = (numpy.concatenate(maps) if maps else
+                               numpy.zeros((0, 3), numpy.int32))
+    save("graphs", **out)
+
+
+def make_tensors(norb, kind, seed):
+    rng = numpy.random.default_rng(1000 + seed)
+    if kind == "real":
+        h1, h2, _ = synthetic.integrals(norb, 2 * norb, seed)
+        return h1, h2
+    if kind in ("complex", "nonsym"):
+        h1 = rng.normal(size=(norb, norb)) + 1j * rng.normal(size=(norb, norb))
+        h2 = (rng.normal(size=(norb,) * 4) + 1j * rng.normal(size=(norb,) * 4)) * 0.3
+        if kind == "complex":  # hermitian h1, h2 with the hermitian pair symmetry
+            h1 = 0.5 * (h1 + h1.conj().T)
+            h2 = 0.5 * (h2 + numpy.einsum("ijkl->lkji", h2.conj()))
+        return h1, h2
+    if kind == "onebody":
+        h1 = rng.normal(size=(norb, norb))
+        return (0.5 * (h1 + h1.T),)
+    if kind == "onebody_complex":
+        return (rng.normal(size=(norb, norb)) + 1j * rng.normal(size=(norb, norb)),)
+    raise ValueError(kind)
+
+
+def apply_fixture():
+    out = {}
+    for norb, na, nb, kind, seed in APPLY_CASES:
+        tensors = make_tensors(norb, kind, seed)
+        d = FqeData(na, nb, norb)
+        rng = numpy.random.default_rng(2000 + seed)
+        c = synthetic.wavefunction_coeff(d.lena(), d.lenb(), rng)
+        d.coeff = c.copy()
+        res = d.apply(tensors).coeff
+        tag = f"{norb}_{na}_{nb}_{kind}"
+        out[f"psi_{tag}"] = c
+        out[f"h1_{tag}"] = numpy.asarray(tensors[0], dtype=numpy.complex128)
+        if len(tensors) > 1:
+            out[f"h2_{tag}"] = numpy.asarray(tensors[1], dtype=numpy.complex128)
+        out[f"sigma_{tag}"] = numpy.asarray(res)
+    # Wavefunction.apply with e_0 (wavefunction.py:396-397)
+    norb, na, nb = 5, 2, 2
+    h1, h2, _ = synthetic.integrals(norb, 10, 11)
+    wfn = fqe.Wavefunction([[na + nb, na - nb, norb]])
+    rng = numpy.random.default_rng(2011)
+    c = synthetic.wavefunction_coeff(math.comb(norb, na), math.comb(norb, nb), rng)
+    wfn.set_wfn(strategy="from_data", raw_data={(na + nb, na - nb): c})
+    ham = fqe.get_restricted_hamiltonian((h1, h2), e_0=-1.25)
+    res = wfn.apply(ham)
+    out["e0_psi"] = c
+    out["e0_h1"] = h1
+    out["e0_h2"] = h2
+    out["e0_sigma"] = res.get_coeff((na + nb, na - nb))
+    save("apply", **out)
+
+
+def dc_fixture():
+    out = {}
+    for norb, na, nb, seed in [(6, 3, 2, 0), (8, 4, 4, 1), (5, 0, 2, 2)]:
+        v = synthetic.diagonal_coulomb(norb, seed)
+        rng = numpy.random.default_rng(3000 + seed)
+        vns = rng.normal(size=(norb, norb))  # non-symmetric for the apply
+        f = rng.normal(size=norb)
+        d = FqeData(na, nb, norb)
+        c = synthetic.wavefunction_coeff(d.lena(), d.lenb(), rng)
+        tag = f"{norb}_{na}_{nb}"
+        t = 0.1
+        d.coeff = c.copy()
+        ev = d.evolve_diagonal_coulomb(-1j * t * f, -1j * t * v, inplace=False)
+        d.coeff = c.copy()
+        ap = d.apply_diagonal_coulomb(f.astype(complex), vns.astype(complex),
+                                      inplace=False)
+        # through the public API: time_evolve with a DiagonalCoulomb
+        wfn = fqe.Wavefunction([[na + nb, na - nb, norb]])
+        wfn.set_wfn(strategy="from_data", raw_data={(na + nb, na - nb): c})
+        te = wfn.time_evolve(t, fqe.get_diagonalcoulomb_hamiltonian(v))
+        out.update({f"psi_{tag}": c, f"v_{tag}": v, f"vns_{tag}": vns,
+                    f"f_{tag}": f, f"evolve_{tag}": numpy.asarray(ev),
+                    f"apply_{tag}": numpy.asarray(ap),
+                    f"time_evolve_{tag}": te.get_coeff((na + nb, na - nb))})
+    save("diagonal_coulomb", **out)
+
+
+def taylor_fixture():
+    out = {}
+    for norb, na, nb, t, acc, seed in [(6, 2, 2, 0.05, 1e-12, 0),
+                                       (8, 4, 4, 0.05, 1e-12, 0),
+                                       (5, 3, 1, 0.3, 1e-15, 1)]:
+        h1, h2, rng = synthetic.integrals(norb, 2 * norb, seed)
+        c = synthetic.wavefunction_coeff(math.comb(norb, na), math.comb(norb, nb), rng)
+        wfn = fqe.Wavefunction([[na + nb, na - nb, norb]])
+        wfn.set_wfn(strategy="from_data", raw_data={(na + nb, na - nb): c})
+        ham = fqe.get_restricted_hamiltonian((h1, h2))
+        res = wfn.apply_generated_unitary(t, "taylor", ham, accuracy=acc)
+        tag = f"{norb}_{na}_{nb}"
+        out.update({f"psi_{tag}": c, f"h1_{tag}": h1, f"h2_{tag}": h2,
+                    f"t_{tag}": numpy.array(t), f"acc_{tag}": numpy.array(acc),
+                    f"out_{tag}": res.get_coeff((na + nb, na - nb))})
+    save("taylor", **out)
+
+
+def dvec_fixture():
+    out = {}
+    for norb, na, nb, seed in [(4, 2, 1, 0), (5, 2, 2, 1)]:
+        d = FqeData(na, nb, norb)
+        rng = numpy.random.default_rng(4000 + seed)
+        c = synthetic.wavefunction_coeff(d.lena(), d.lenb(), rng)
+        d.coeff = c.copy()
+        dv = d.calculate_dvec_spatial()
+        co = d._calculate_coeff_spatial_with_dvec(dv)
+        tag = f"{norb}_{na}_{nb}"
+        out.update({f"psi_{tag}": c, f"dvec_{tag}": dv, f"coeff_{tag}": co})
+    save("dvec", **out)
+
+
+if __name__ == "__main__":
+    graph_fixture()
+    apply_fixture()
+    dc_fixture()
+    taylor_fixture()
+    dvec_fixture()

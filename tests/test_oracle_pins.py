@@ -1,0 +1,194 @@
+"""Pins the CPU oracle (oracle/) to the reference.
+
+* against tests/golden/*.npz, produced by running the reference FQE 0.3.0
+  (tests/golden/make_golden.py) — always runs;
+* against the reference's own golden data (tests/unittest_data/fqe_data of
+  the reference, read in place) and known-answer tests — when the reference
+  tree is mounted;
+* against the live reference (imported with oracle/ref_fqe.py) on extra
+  seeded cases — when its natives are built in oracle/_ref.
+"""
+
+import math
+import os
+
+import numpy
+import pytest
+
+import ref_fqe
+
+REF_DATA = os.path.join(ref_fqe.REF_ROOT, "tests", "unittest_data")
+
+
+def _rel(a, b):
+    return numpy.linalg.norm(a - b) / max(numpy.linalg.norm(b), 1e-300)
+
+
+def test_graph_tables_match_fixture(golden, oracle):
+    gd = golden("graphs")
+    for key in [k for k in gd if k.startswith("astr_")]:
+        tag = key[5:]
+        norb, na, nb = map(int, tag.split("_"))
+        g = oracle.graph(norb, na, nb)
+        numpy.testing.assert_array_equal(g.astr, gd["astr_" + tag])
+        numpy.testing.assert_array_equal(g.bstr, gd["bstr_" + tag])
+        numpy.testing.assert_array_equal(g.dexca, gd["dexca_" + tag])
+        numpy.testing.assert_array_equal(g.dexcb, gd["dexcb_" + tag])
+        numpy.testing.assert_array_equal(g.alens.ravel(), gd["amaplen_" + tag])
+        numpy.testing.assert_array_equal(g.amaps, gd["amaps_" + tag])
+
+
+def test_string_order_known_answer(oracle):
+    # tests/fci_graph_test.py:34-39 of the reference: the 70 strings of
+    # (4 electrons, 8 orbitals) in address order begin 15, 23, 39, 71, 135 and
+    # end 216, 232, 240; address(27) = 5, address(30) = 35.
+    s = oracle.strings(8, 4)
+    assert list(s[:5]) == [15, 23, 39, 71, 135]
+    assert list(s[-3:]) == [216, 232, 240]
+    assert list(s).index(27) == 5 and list(s).index(30) == 35
+    assert len(set(s.tolist())) == 70 and all(bin(int(x)).count("1") == 4 for x in s)
+
+
+def _apply_cases(gd):
+    for key in [k for k in gd if k.startswith("sigma_")]:
+        tag = key[6:]
+        norb, na, nb = map(int, tag.split("_")[:3])
+        tensors = (gd["h1_" + tag],) + ((gd["h2_" + tag],) if "h2_" + tag in gd else ())
+        yield tag, norb, na, nb, tensors, gd["psi_" + tag], gd[key]
+
+
+def test_apply_matches_fixture(golden, oracle):
+    gd = golden("apply")
+    n = 0
+    for tag, norb, na, nb, tensors, psi, sigma in _apply_cases(gd):
+        g = oracle.graph(norb, na, nb)
+        out = oracle.apply_restricted(psi, tensors, 0.0, g)
+        assert _rel(out, sigma) < 1e-13, tag
+        n += 1
+    assert n >= 8
+    g = oracle.graph(5, 2, 2)
+    out = oracle.apply_restricted(gd["e0_psi"], (gd["e0_h1"], gd["e0_h2"]), -1.25, g)
+    assert _rel(out, gd["e0_sigma"]) < 1e-13
+
+
+def test_diagonal_coulomb_matches_fixture(golden, oracle):
+    gd = golden("diagonal_coulomb")
+    for key in [k for k in gd if k.startswith("evolve_")]:
+        tag = key[7:]
+        norb, na, nb = map(int, tag.split("_"))
+        g = oracle.graph(norb, na, nb)
+        psi, v, f = gd["psi_" + tag], gd["v_" + tag], gd["f_" + tag]
+        ev = oracle.evolve_diagonal_coulomb(psi, -1j * 0.1 * f, -1j * 0.1 * v, g)
+        assert _rel(ev, gd[key]) < 1e-13
+        ap = oracle.apply_diagonal_coulomb(psi, f, gd["vns_" + tag], g)
+        assert _rel(ap, gd["apply_" + tag]) < 1e-13
+        te = oracle.evolve_diagonal_coulomb(psi, numpy.zeros(norb, complex),
+                                            -1j * 0.1 * v, g)
+        assert _rel(te, gd["time_evolve_" + tag]) < 1e-13
+
+
+def test_taylor_matches_fixture(golden, oracle):
+    gd = golden("taylor")
+    for key in [k for k in gd if k.startswith("out_")]:
+        tag = key[4:]
+        norb, na, nb = map(int, tag.split("_"))
+        g = oracle.graph(norb, na, nb)
+        out, _ = oracle.taylor_evolve(gd["psi_" + tag], (gd["h1_" + tag], gd["h2_" + tag]),
+                                      0.0, float(gd["t_" + tag]), g,
+                                      accuracy=float(gd["acc_" + tag]))
+        assert _rel(out, gd[key]) < 1e-12
+
+
+def test_dvec_matches_fixture(golden, oracle):
+    gd = golden("dvec")
+    for key in [k for k in gd if k.startswith("dvec_")]:
+        tag = key[5:]
+        norb, na, nb = map(int, tag.split("_"))
+        g = oracle.graph(norb, na, nb)
+        dv = oracle.make_dvec(gd["psi_" + tag], g)
+        numpy.testing.assert_allclose(dv, gd[key], rtol=0, atol=1e-15)
+        co = oracle.make_coeff(dv, g)
+        assert _rel(co, gd["coeff_" + tag]) < 1e-14
+
+
+def test_known_eigenvalue_2_body(oracle):
+    # tests/fqe_data_test.py:761-827 of the reference: h2[i,j,k,l] =
+    # (i+k)(j+l) * 0.02 on (2 alpha, 2 beta, 4 orbitals) has the eigenvalue
+    # -7.271991091302982.  The lowest eigenvalue of H on the sector must be it.
+    norb = 4
+    idx = numpy.arange(norb)
+    h2 = (idx[:, None, None, None] + idx[None, None, :, None]) * \
+         (idx[None, :, None, None] + idx[None, None, None, :]) * 0.02
+    h1 = numpy.zeros((norb, norb))
+    g = oracle.graph(norb, 2, 2)
+    H = oracle.dense_hamiltonian(h1, h2.astype(complex), g)
+    w = numpy.linalg.eigvals(H)
+    assert numpy.min(numpy.abs(w - (-7.271991091302982))) < 1e-10
+
+
+def _ref_golden_available():
+    return os.path.isdir(os.path.join(REF_DATA, "fqe_data"))
+
+
+@pytest.mark.skipif(not _ref_golden_available(),
+                    reason="reference golden data not mounted")
+@pytest.mark.parametrize("na,nb,norb", [(2, 3, 6), (2, 1, 4), (1, 1, 2)])
+def test_reference_golden_apply(oracle, na, nb, norb):
+    # tests/unittest_data/fqe_data/{cr,ci}NNNNNN{,_1,_12} + hN files
+    # (written by tests/unittest_data/fqe_data/generate_data.py)
+    tag = f"{na:02d}{nb:02d}{norb:02d}"
+    base = os.path.join(REF_DATA, "fqe_data")
+    g = oracle.graph(norb, na, nb)
+    shape = (g.lena, g.lenb)
+
+    def cplx(stem):
+        cr = numpy.fromfile(os.path.join(base, "cr" + stem + ".npy")).reshape(shape)
+        ci = numpy.fromfile(os.path.join(base, "ci" + stem + ".npy")).reshape(shape)
+        return cr + 1j * ci
+
+    psi = cplx(tag)
+    h1 = numpy.fromfile(os.path.join(base, f"h1{tag}.npy")).reshape((norb,) * 2)
+    h2 = numpy.fromfile(os.path.join(base, f"h2{tag}.npy")).reshape((norb,) * 4)
+    assert _rel(oracle.apply_spatial1(psi, h1, g), cplx(tag + "_1")) < 1e-13
+    assert _rel(oracle.apply_spatial12(psi, h1 * 0, h2, g), cplx(tag + "_2")) < 1e-13
+    assert _rel(oracle.apply_spatial12(psi, h1, h2, g), cplx(tag + "_12")) < 1e-13
+
+
+@pytest.mark.skipif(not _ref_golden_available(),
+                    reason="reference golden data not mounted")
+@pytest.mark.parametrize("na,nb,norb", [(2, 3, 6), (2, 1, 4)])
+def test_reference_golden_diagonal_coulomb(oracle, na, nb, norb):
+    # fqe_data_test.py:268-280: evolve with dmat at t = 0.1, golden _dc
+    tag = f"{na:02d}{nb:02d}{norb:02d}"
+    base = os.path.join(REF_DATA, "fqe_data")
+    g = oracle.graph(norb, na, nb)
+    shape = (g.lena, g.lenb)
+
+    def cplx(stem):
+        cr = numpy.fromfile(os.path.join(base, "cr" + stem + ".npy")).reshape(shape)
+        ci = numpy.fromfile(os.path.join(base, "ci" + stem + ".npy")).reshape(shape)
+        return cr + 1j * ci
+
+    dmat = numpy.fromfile(os.path.join(base, f"dmat{tag}.npy")).reshape(norb, norb)
+    t = 0.1
+    out = oracle.evolve_diagonal_coulomb(cplx(tag), numpy.zeros(norb, complex),
+                                         -1j * t * dmat.astype(complex), g)
+    assert _rel(out, cplx(tag + "_dc")) < 1e-13
+
+
+@pytest.mark.skipif(not ref_fqe.available(), reason="reference natives not built")
+def test_live_reference_random_cases(oracle):
+    fqe = ref_fqe.import_fqe()
+    from fqe.fqe_data import FqeData
+    rng = numpy.random.default_rng(99)
+    for norb, na, nb in [(3, 1, 2), (5, 3, 3), (6, 2, 4), (7, 4, 2), (8, 1, 1)]:
+        h1 = rng.normal(size=(norb,) * 2) + 1j * rng.normal(size=(norb,) * 2)
+        h2 = rng.normal(size=(norb,) * 4) + 1j * rng.normal(size=(norb,) * 4)
+        d = FqeData(na, nb, norb)
+        c = rng.normal(size=d.coeff.shape) + 1j * rng.normal(size=d.coeff.shape)
+        d.coeff = c.copy()
+        ref = d.apply((h1, h2)).coeff
+        g = oracle.graph(norb, na, nb)
+        assert _rel(oracle.apply_spatial12(c, h1, h2, g), ref) < 1e-13
+        numpy.testing.assert_array_equal(g.dexca, d._core._dexca)
+        numpy.testing.assert_array_equal(g.astr, d._core._astr)
