@@ -247,6 +247,11 @@ int launch_scatter(const fqegpu_graph_s* g, bool tri, int P, int64_t c0,
                    double2 alpha, double2 beta, bool init, double2* sigma,
                    cudaStream_t st) {
   const int64_t lena = g->a.len, lenb = g->b.len;
+  if (lena > 65535) {
+    set_error("alpha string space of %lld exceeds the 65535 rows one launch covers",
+              (long long)lena);
+    return FQEGPU_ERR_UNSUPPORTED;
+  }
   dim3 grid((unsigned)((lenb + 255) / 256), (unsigned)lena);
   k_scatter<0><<<grid, 256, 0, st>>>(P, lena, lenb, c0, w, tab_of(g->a, tri),
                                      tab_of(g->b, tri), G, psi, nullptr, nullptr,
@@ -288,6 +293,11 @@ int apply_fp64(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
     k_axpby<<<grid_1d(N), 256, 0, st>>>(N, beta, psi, sigma);
     FQE_CUDA(cudaGetLastError());
     return FQEGPU_OK;
+  }
+  if (lena > 65535) {
+    set_error("alpha string space of %lld exceeds the 65535 rows one launch covers",
+              (long long)lena);
+    return FQEGPU_ERR_UNSUPPORTED;
   }
   if (h->onebody) {
     dim3 grid((unsigned)((lenb + 255) / 256), (unsigned)lena);
