@@ -57,6 +57,9 @@ struct fqegpu_ham_s {
 };
 
 namespace fqegpu {
+inline double2 zmul_host(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
 // Records event k of block `blk` when timing is on (no-op otherwise).
 int stage_mark(fqegpu_ham h, int blk, int k, cudaStream_t st);
 int apply_fp64(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,

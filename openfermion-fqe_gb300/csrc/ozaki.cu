@@ -1,15 +1,638 @@
-// Tensor-core (tcgen05) contraction with Ozaki splitting — placeholder until
-// the kernel lands; the FP64 path is the reference-exact drop-in.
+// Tensor-core pair contraction with Ozaki splitting (FQEGPU_PREC_OZAKI).
+//
+// G[p][I] = sum_q V[p][q] D[q][I] with V the real pair matrix (fqe_data.py
+// :658-681 compressed form, one-body part folded in) and D[q][I] = <I|E_q|psi>.
+// GB300's FP64 pipe runs at ~1.1 TFLOP/s, so the FP64 operands are split into
+// BF16 slices and contracted on the 5th-generation tensor cores:
+//
+//   V[p][q] = 2^{eV(p)} sum_{k=1..5} v_k[p][q] 2^{-8k},  v_k in {-255..255}
+//   D[q][I] = 2^{E(I)}  sum_{k=1..5} d_k[q][I] 2^{-8k},  d_k in {-255..255}
+//
+// (sign-magnitude bytes of 40-bit fixed-point values; eV(p) bounds row p of V,
+// E(I) bounds column I of D).  Every slice is stored as its true value
+// (byte * 2^{-8k}, exact in BF16), so every product lands on one absolute
+// scale and the products are grouped by level L = a + b into three TMEM
+// accumulators: L = 2 and L = 3 sum integers times 2^{-8L} below 2^24 and are
+// exact in FP32; L = 4..6 share one accumulator whose FP32 rounding sits
+// 2^-40 below the leading term.  Levels >= 7 are dropped (also ~2^-40).  The
+// three accumulators are combined into an FP32 pair (hi + lo, ~48 bits) and
+// scaled by 2^{eV(p) + E(I)}.
+//
+// D is never written to HBM: producer warps gather it from a 62-bit
+// fixed-point copy of psi (global scale) through the per-pair target tables,
+// cut it into slices and store them in the canonical no-swizzle K-major
+// layout in shared memory.  One thread issues tcgen05.mma; four epilogue
+// warps drain the accumulators (double-buffered in TMEM) into G, stored as
+// FP32 pairs [P][lena][lenb].  The scatter then runs in FP32-pair arithmetic.
+//
+// Persistent kernel, one CTA per SM, 13 warps:
+//   warps 0-3  epilogue (warp w reads TMEM lanes 32w..32w+31 = pairs p)
+//   warp 4     TMEM allocation; lane 0 issues the MMAs
+//   warps 5-12 producers
+// Tiles are 32 determinants of one alpha row (64 real columns = MMA N),
+// visited in column super-blocks of 1024 so the alpha-source rows stay in L2.
+// Every wait is bounded; on a timeout the kernel records an error, lets the
+// other roles leave, and frees its TMEM.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "ham.cuh"
+#include "tcgen05.cuh"
 
 namespace fqegpu {
-struct OzakiPlan {};
+
+namespace {
+constexpr int kSlices = 5;
+constexpr int kM = 128;        // MMA M (pairs, padded)
+constexpr int kN = 64;         // MMA N (real columns per tile)
+constexpr int kDets = 32;      // determinants per tile
+constexpr int kRing = 4;       // D-slice ring depth
+constexpr int kSuperBlocks = 32;
+constexpr int kEpiWarps = 4;
+constexpr int kMmaWarp = 4;
+constexpr int kProdWarps = 8;
+constexpr int kThreads = (kEpiWarps + 1 + kProdWarps) * 32;
+constexpr int kAccCols = 3 * kN;  // one accumulator set
+constexpr uint32_t kTmemCols = 512;
+constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
+constexpr int kExpZero = -2000;
+}  // namespace
+
+struct OzakiPlan {
+  int P = 0, KP = 0;
+  __nv_bfloat16* d_vslices = nullptr;  // [5][128 * KP] canonical K-major
+  int32_t* d_vexp = nullptr;           // [128]
+  longlong2* d_psix = nullptr;         // [N]
+  int32_t* d_rowexp = nullptr;         // [lena]
+  int32_t* d_colexp = nullptr;         // [lenb]
+  int32_t* d_misc = nullptr;           // [0] = global exponent, [1] = error
+  float4* d_G = nullptr;               // [P][N]
+  int nsm = 0;
+  size_t smem = 0;
+};
+
+struct OzArgs {
+  int P, KP;
+  int64_t lena, lenb, ntiles;
+  int nb;  // column blocks per row
+  const int32_t* tabA;
+  const int32_t* tabB;
+  const longlong2* psix;
+  const int32_t* rowexp;
+  const int32_t* colexp;
+  const int32_t* misc;
+  const __nv_bfloat16* vslices;
+  const int32_t* vexp;
+  float4* G;
+  int32_t* err;
+};
+
+// Tile t -> (alpha row, first beta column) with column super-blocks.
+__device__ __forceinline__ void tile_coords(const OzArgs& A, int64_t t, int64_t& ia,
+                                            int64_t& ib0) {
+  const int64_t per_sb = A.lena * kSuperBlocks;
+  const int64_t s = t / per_sb;
+  const int64_t r = t - s * per_sb;
+  const int64_t ws = min((int64_t)kSuperBlocks, (int64_t)A.nb - s * kSuperBlocks);
+  ia = r / ws;
+  ib0 = (s * kSuperBlocks + (r - ia * ws)) * kDets;
+}
+
+// Bounded wait that also gives up when another role has aborted.
+__device__ __forceinline__ bool oz_wait(uint64_t* bar, uint32_t parity,
+                                        volatile int* abort_flag) {
+  const long long t0 = clock64();
+  for (uint32_t it = 0;; ++it) {
+    if (tc::mbar_try_wait(bar, parity)) return true;
+    if ((it & 255u) == 255u) {
+      if (*abort_flag) return false;
+      if (clock64() - t0 > kWaitCycles) return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void oz_abort(volatile int* abort_flag, int32_t* err, int code) {
+  *abort_flag = 1;
+  atomicExch(err, code);
+}
+
+__device__ __forceinline__ int det_exponent(const OzArgs& A, int64_t ia, int64_t ib) {
+  return max(A.rowexp[ia], A.colexp[ib]) + 1;
+}
+
+// 40-bit magnitude of x * 2^-sh (x fixed point), sign separate.
+__device__ __forceinline__ uint64_t mag40(long long x, int sh, uint32_t& neg) {
+  neg = x < 0 ? 1u : 0u;
+  uint64_t m = (uint64_t)(x < 0 ? -x : x);
+  if (sh >= 0) {
+    m = sh >= 64 ? 0ull : (m >> sh);
+  } else {
+    m = (-sh >= 64) ? 0ull : (m << (-sh));
+  }
+  return m & ((1ull << 40) - 1ull);
+}
+
+__device__ __forceinline__ uint32_t bf16_slice_pair(uint64_t m0, uint32_t n0,
+                                                    uint64_t m1, uint32_t n1,
+                                                    int shift, float scale) {
+  const float f0 = (float)(uint32_t)((m0 >> shift) & 0xFFull) * (n0 ? -scale : scale);
+  const float f1 = (float)(uint32_t)((m1 >> shift) & 0xFFull) * (n1 ? -scale : scale);
+  const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int KP = A.KP;
+  const uint32_t v_elems = (uint32_t)kM * KP;
+  const uint32_t slot_elems = (uint32_t)kN * KP;
+  __nv_bfloat16* sV = reinterpret_cast<__nv_bfloat16*>(smem);
+  __nv_bfloat16* sD = sV + kSlices * v_elems;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sD + kRing * slot_elems);
+  uint64_t* empty = full + kRing;
+  uint64_t* accfull = empty + kRing;
+  uint64_t* accempty = accfull + 2;
+  uint64_t* done = accempty + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  {
+    const int4* src = reinterpret_cast<const int4*>(A.vslices);
+    int4* dst = reinterpret_cast<int4*>(sV);
+    const int n16 = (int)(kSlices * v_elems * 2 / 16);
+    for (int i = tid; i < n16; i += blockDim.x) dst[i] = src[i];
+  }
+  if (tid == 0) {
+    for (int i = 0; i < kRing; ++i) {
+      tc::mbar_init(&full[i], kProdWarps);
+      tc::mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&accfull[i], 1);
+      tc::mbar_init(&accempty[i], kEpiWarps);
+    }
+    tc::mbar_init(done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc::fence_proxy_async_smem();
+  __syncthreads();
+  if (warp == kMmaWarp) tc::tmem_alloc(tslot, kTmemCols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const int64_t stride = gridDim.x;
+
+  if (warp == kMmaWarp) {
+    if (lane == 0) {
+      const uint32_t idesc = tc::make_idesc_bf16(kM, kN);
+      const uint32_t sbo = (uint32_t)KP * 16u;
+      const int ksteps = KP / 16;
+      int64_t it = 0;
+      for (int64_t t = blockIdx.x; t < A.ntiles; t += stride, ++it) {
+        const int s = (int)(it & 1);
+        if (!oz_wait(&accempty[s], (uint32_t)(((it >> 1) & 1) ^ 1), abort_flag)) {
+          oz_abort(abort_flag, A.err, 2);
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t acc0 = tmem + (uint32_t)(s * kAccCols);
+        bool first[3] = {true, true, true};
+        bool ok = true;
+        for (int b = 1; b <= kSlices && ok; ++b) {
+          const int64_t g = it * kSlices + (b - 1);
+          const int slot = (int)(g % kRing);
+          if (!oz_wait(&full[slot], (uint32_t)((g / kRing) & 1), abort_flag)) {
+            oz_abort(abort_flag, A.err, 3);
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint32_t bbase = tc::smem_u32(sD + (size_t)slot * slot_elems);
+          for (int a = 1; a <= kSlices + 1 - b; ++a) {
+            const int lvl = a + b;
+            const int ai = lvl == 2 ? 0 : (lvl == 3 ? 1 : 2);
+            const uint32_t acc = acc0 + (uint32_t)(ai * kN);
+            const uint32_t abase = tc::smem_u32(sV + (size_t)(a - 1) * v_elems);
+            for (int ks = 0; ks < ksteps; ++ks) {
+              const uint64_t ad = tc::make_sdesc(abase + ks * 256, 128, sbo);
+              const uint64_t bd = tc::make_sdesc(bbase + ks * 256, 128, sbo);
+              tc::mma_bf16(acc, ad, bd, idesc, (first[ai] && ks == 0) ? 0u : 1u);
+            }
+            first[ai] = false;
+          }
+          tc::mma_commit(&empty[slot]);
+        }
+        if (!ok) break;
+        tc::mma_commit(&accfull[s]);
+      }
+      // every MMA issued above has completed before TMEM is released
+      tc::mma_commit(done);
+      if (!oz_wait(done, 0, abort_flag) && !*abort_flag) oz_abort(abort_flag, A.err, 6);
+    }
+  } else if (warp < kEpiWarps) {
+    const int p = tid;  // TMEM lane = pair row
+    const int ev = (p < A.P) ? A.vexp[p] : 0;
+    int64_t it = 0;
+    for (int64_t t = blockIdx.x; t < A.ntiles; t += stride, ++it) {
+      int64_t ia, ib0;
+      tile_coords(A, t, ia, ib0);
+      const int s = (int)(it & 1);
+      const bool got = __all_sync(0xffffffffu,
+                                  oz_wait(&accfull[s], (uint32_t)((it >> 1) & 1), abort_flag));
+      if (!got) {
+        if (lane == 0) oz_abort(abort_flag, A.err, 4);
+        break;
+      }
+      tc::fence_after_sync();
+      const uint32_t base = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(s * kAccCols);
+      const int rexp = A.rowexp[ia];
+      for (int c0 = 0; c0 < kN; c0 += 16) {
+        float va[16], vb[16], vc[16];
+        tc::tmem_ld16(base + c0, va);
+        tc::tmem_ld16(base + kN + c0, vb);
+        tc::tmem_ld16(base + 2 * kN + c0, vc);
+        if (p >= A.P) continue;
+#pragma unroll
+        for (int j = 0; j < 16; j += 2) {
+          const int64_t ib = ib0 + (c0 + j) / 2;
+          if (ib >= A.lenb) continue;
+          const int sc = ev + max(rexp, A.colexp[ib]) + 1;
+          float out[4];
+#pragma unroll
+          for (int part = 0; part < 2; ++part) {
+            const float x = va[j + part], y = vb[j + part], z = vc[j + part];
+            // exact two-sum of the exact levels, then the rounded remainder
+            const float h = x + y;
+            const float bb = h - x;
+            float l = (x - (h - bb)) + (y - bb);
+            l += z;
+            const float h2 = h + l;
+            const float l2 = l - (h2 - h);
+            out[2 * part] = ldexpf(h2, sc);
+            out[2 * part + 1] = ldexpf(l2, sc);
+          }
+          A.G[((int64_t)p * A.lena + ia) * A.lenb + ib] =
+              make_float4(out[0], out[1], out[2], out[3]);
+        }
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&accempty[s]);
+    }
+  } else {
+    const int pw = warp - (kEpiWarps + 1);  // 0..7
+    const int noct = KP / 8;
+    const int g0 = A.misc[0];
+    int64_t it = 0;
+    for (int64_t t = blockIdx.x; t < A.ntiles; t += stride, ++it) {
+      int64_t ia, ib0;
+      tile_coords(A, t, ia, ib0);
+      const int64_t ib = ib0 + lane;
+      const bool valid = ib < A.lenb;
+      const int sh = valid ? 22 + det_exponent(A, ia, ib) - g0 : 0;
+      uint64_t mre[2][8], mim[2][8];
+      uint32_t nre[2], nim[2];
+#pragma unroll
+      for (int oi = 0; oi < 2; ++oi) {
+        nre[oi] = nim[oi] = 0u;
+        const int o = pw + 8 * oi;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          long long re = 0, im = 0;
+          const int q = 8 * o + j;
+          if (o < noct && valid && q < A.P) {
+            const int32_t ca = A.tabA[(int64_t)q * A.lena + ia];
+            const int32_t cb = A.tabB[(int64_t)q * A.lenb + ib];
+            if (ca) {
+              const longlong2 x = A.psix[(int64_t)(abs(ca) - 1) * A.lenb + ib];
+              if (ca > 0) { re += x.x; im += x.y; } else { re -= x.x; im -= x.y; }
+            }
+            if (cb) {
+              const longlong2 x = A.psix[ia * A.lenb + (abs(cb) - 1)];
+              if (cb > 0) { re += x.x; im += x.y; } else { re -= x.x; im -= x.y; }
+            }
+          }
+          uint32_t n;
+          mre[oi][j] = mag40(re, sh, n);
+          nre[oi] |= n << j;
+          mim[oi][j] = mag40(im, sh, n);
+          nim[oi] |= n << j;
+        }
+      }
+      bool ok = true;
+      for (int b = 1; b <= kSlices; ++b) {
+        const int64_t g = it * kSlices + (b - 1);
+        const int slot = (int)(g % kRing);
+        const bool got = __all_sync(
+            0xffffffffu, oz_wait(&empty[slot], (uint32_t)(((g / kRing) & 1) ^ 1), abort_flag));
+        if (!got) {
+          if (lane == 0) oz_abort(abort_flag, A.err, 5);
+          ok = false;
+          break;
+        }
+        __nv_bfloat16* sb = sD + (size_t)slot * slot_elems;
+        const int shift = 40 - 8 * b;
+        const float scale = ldexpf(1.0f, -8 * b);
+#pragma unroll
+        for (int oi = 0; oi < 2; ++oi) {
+          const int o = pw + 8 * oi;
+          if (o >= noct) continue;
+#pragma unroll
+          for (int part = 0; part < 2; ++part) {
+            const uint64_t* m = part ? mim[oi] : mre[oi];
+            const uint32_t nb = part ? nim[oi] : nre[oi];
+            uint4 v;
+            v.x = bf16_slice_pair(m[0], nb & 1u, m[1], (nb >> 1) & 1u, shift, scale);
+            v.y = bf16_slice_pair(m[2], (nb >> 2) & 1u, m[3], (nb >> 3) & 1u, shift, scale);
+            v.z = bf16_slice_pair(m[4], (nb >> 4) & 1u, m[5], (nb >> 5) & 1u, shift, scale);
+            v.w = bf16_slice_pair(m[6], (nb >> 6) & 1u, m[7], (nb >> 7) & 1u, shift, scale);
+            *reinterpret_cast<uint4*>(sb + tc::kmajor_offset(2 * lane + part, 8 * o, KP)) = v;
+          }
+        }
+        tc::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&full[slot]);
+      }
+      if (!ok) break;
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == kMmaWarp) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+// ---- pre-pass: exponent bounds and the fixed-point copy of psi ------------
+__device__ __forceinline__ int exp_of(double x) {
+  // e with |x| < 2^e (frexp convention); kExpZero for 0
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int be = (int)((b >> 52) & 0x7FF);
+  if (be == 0) return (b << 1) == 0 ? kExpZero : -1022;  // subnormals: bound
+  return be - 1022;
+}
+
+__global__ void k_oz_rowexp(int64_t lenb, const double2* __restrict__ psi,
+                            int32_t* __restrict__ rowexp) {
+  __shared__ int red[256];
+  const int64_t a = blockIdx.x;
+  int e = kExpZero;
+  for (int64_t b = threadIdx.x; b < lenb; b += blockDim.x) {
+    const double2 v = psi[a * lenb + b];
+    e = max(e, max(exp_of(v.x), exp_of(v.y)));
+  }
+  red[threadIdx.x] = e;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = max(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) rowexp[a] = red[0];
+}
+
+__global__ void k_oz_colexp_init(int64_t lenb, int32_t* __restrict__ colexp) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b < lenb) colexp[b] = kExpZero;
+}
+
+// grid (column blocks, row chunks): each thread folds a chunk of rows of one
+// column, then one atomicMax per thread.
+__global__ void k_oz_colexp(int64_t lena, int64_t lenb, const double2* __restrict__ psi,
+                            int32_t* __restrict__ colexp) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= lenb) return;
+  const int64_t chunk = (lena + gridDim.y - 1) / gridDim.y;
+  const int64_t a0 = blockIdx.y * chunk, a1 = min(lena, a0 + chunk);
+  int e = kExpZero;
+  for (int64_t a = a0; a < a1; ++a) {
+    const double2 v = psi[a * lenb + b];
+    e = max(e, max(exp_of(v.x), exp_of(v.y)));
+  }
+  atomicMax(&colexp[b], e);
+}
+
+__global__ void k_oz_globalexp(int64_t lena, const int32_t* __restrict__ rowexp,
+                               int32_t* __restrict__ misc) {
+  __shared__ int red[256];
+  int e = kExpZero;
+  for (int64_t a = threadIdx.x; a < lena; a += blockDim.x) e = max(e, rowexp[a]);
+  red[threadIdx.x] = e;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = max(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    misc[0] = red[0];
+    misc[1] = 0;
+  }
+}
+
+// psix = round(psi * 2^(62 - g0)), |psix| < 2^62.
+__global__ void k_oz_fixed(int64_t n, const double2* __restrict__ psi,
+                           const int32_t* __restrict__ misc,
+                           longlong2* __restrict__ psix) {
+  const int g0 = misc[0];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    longlong2 o = make_longlong2(0, 0);
+    if (g0 > kExpZero) {
+      const double2 v = psi[i];
+      o.x = __double2ll_rn(ldexp(v.x, 62 - g0));
+      o.y = __double2ll_rn(ldexp(v.y, 62 - g0));
+    }
+    psix[i] = o;
+  }
+}
+
+// ---- scatter in FP32-pair arithmetic ----------------------------------------
+__device__ __forceinline__ void df_add(float& h, float& l, float bh, float bl) {
+  const float s = h + bh;
+  const float v = s - h;
+  float e = (h - (s - v)) + (bh - v);
+  e += l + bl;
+  h = s + e;
+  l = e - (h - s);
+}
+
+__device__ __forceinline__ double2 zmul2(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__global__ void __launch_bounds__(256) k_oz_scatter(
+    int P, int64_t lena, int64_t lenb, const int32_t* __restrict__ tabA,
+    const int32_t* __restrict__ tabB, const float4* __restrict__ G,
+    const double2* __restrict__ psi, double2 alpha, double2 beta,
+    double2* __restrict__ sigma) {
+  const int64_t a = blockIdx.y;
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= lenb) return;
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+  for (int p = 0; p < P; ++p) {
+    const int32_t ca = tabA[(int64_t)p * lena + a];
+    if (ca) {
+      float4 g = G[((int64_t)p * lena + (abs(ca) - 1)) * lenb + b];
+      if (ca < 0) g = make_float4(-g.x, -g.y, -g.z, -g.w);
+      df_add(rh, rl, g.x, g.y);
+      df_add(ih, il, g.z, g.w);
+    }
+    const int32_t cb = tabB[(int64_t)p * lenb + b];
+    if (cb) {
+      float4 g = G[((int64_t)p * lena + a) * lenb + (abs(cb) - 1)];
+      if (cb < 0) g = make_float4(-g.x, -g.y, -g.z, -g.w);
+      df_add(rh, rl, g.x, g.y);
+      df_add(ih, il, g.z, g.w);
+    }
+  }
+  const int64_t I = a * lenb + b;
+  const double2 acc = make_double2((double)rh + (double)rl, (double)ih + (double)il);
+  double2 out = zmul2(alpha, acc);
+  if (beta.x != 0.0 || beta.y != 0.0) {
+    const double2 t = zmul2(beta, psi[I]);
+    out.x += t.x;
+    out.y += t.y;
+  }
+  sigma[I] = out;
+}
+
+// ---- host ---------------------------------------------------------------------
+static int plan_create(fqegpu_ham h) {
+  auto* pl = new (std::nothrow) OzakiPlan();
+  if (!pl) {
+    set_error("host allocation failed");
+    return FQEGPU_ERR_NOMEM;
+  }
+  h->oz = pl;
+  const int P = h->P;
+  const int KP = (P + 15) / 16 * 16;
+  pl->P = P;
+  pl->KP = KP;
+  const size_t vel = (size_t)kM * KP;
+  std::vector<__nv_bfloat16> sl(kSlices * vel, __float2bfloat16(0.0f));
+  std::vector<int32_t> vexp(kM, 0);
+  for (int p = 0; p < P; ++p) {
+    double mx = 0.0;
+    for (int q = 0; q < P; ++q) mx = std::max(mx, std::fabs(h->vpair[(size_t)p * P + q]));
+    if (mx == 0.0) continue;
+    int e;
+    std::frexp(mx, &e);  // mx < 2^e
+    vexp[p] = e;
+    for (int q = 0; q < P; ++q) {
+      const double v = h->vpair[(size_t)p * P + q];
+      const double y = std::floor(std::ldexp(std::fabs(v), 40 - e));
+      const uint64_t m = (uint64_t)y;
+      for (int k = 1; k <= kSlices; ++k) {
+        const uint32_t byte = (uint32_t)((m >> (40 - 8 * k)) & 0xFFu);
+        const float f = std::ldexp((float)byte, -8 * k) * (v < 0 ? -1.0f : 1.0f);
+        sl[(size_t)(k - 1) * vel + tc::kmajor_offset(p, q, KP)] = __float2bfloat16(f);
+      }
+    }
+  }
+  FQE_CUDA(cudaMalloc(&pl->d_vslices, sizeof(__nv_bfloat16) * sl.size()));
+  FQE_CUDA(cudaMemcpy(pl->d_vslices, sl.data(), sizeof(__nv_bfloat16) * sl.size(),
+                      cudaMemcpyHostToDevice));
+  FQE_CUDA(cudaMalloc(&pl->d_vexp, sizeof(int32_t) * kM));
+  FQE_CUDA(cudaMemcpy(pl->d_vexp, vexp.data(), sizeof(int32_t) * kM, cudaMemcpyHostToDevice));
+  const int64_t lena = h->g->a.len, lenb = h->g->b.len, N = lena * lenb;
+  FQE_CUDA(cudaMalloc(&pl->d_psix, sizeof(longlong2) * N));
+  FQE_CUDA(cudaMalloc(&pl->d_rowexp, sizeof(int32_t) * lena));
+  FQE_CUDA(cudaMalloc(&pl->d_colexp, sizeof(int32_t) * lenb));
+  FQE_CUDA(cudaMalloc(&pl->d_misc, sizeof(int32_t) * 4));
+  FQE_CUDA(cudaMalloc(&pl->d_G, sizeof(float4) * (size_t)P * N));
+  int dev = 0;
+  FQE_CUDA(cudaGetDevice(&dev));
+  FQE_CUDA(cudaDeviceGetAttribute(&pl->nsm, cudaDevAttrMultiProcessorCount, dev));
+  pl->smem = sizeof(__nv_bfloat16) * ((size_t)kSlices * vel + (size_t)kRing * kN * KP) +
+             sizeof(uint64_t) * (2 * kRing + 5) + 16;
+  FQE_CUDA(cudaFuncSetAttribute(k_oz_contract, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)pl->smem));
+  return FQEGPU_OK;
+}
+
 void ozaki_destroy(fqegpu_ham h) {
-  delete h->oz;
+  OzakiPlan* pl = h->oz;
+  if (!pl) return;
+  cudaFree(pl->d_vslices);
+  cudaFree(pl->d_vexp);
+  cudaFree(pl->d_psix);
+  cudaFree(pl->d_rowexp);
+  cudaFree(pl->d_colexp);
+  cudaFree(pl->d_misc);
+  cudaFree(pl->d_G);
+  delete pl;
   h->oz = nullptr;
 }
-int apply_ozaki(fqegpu_ham, const double2*, double2*, double2, double2, cudaStream_t) {
-  set_error("tensor-core contraction not built yet");
-  return FQEGPU_ERR_UNSUPPORTED;
+
+int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
+                double2 beta, cudaStream_t st) {
+  // The split needs a real pair matrix that fits one 128-row MMA tile; other
+  // operators run the FP64 kernels on the GPU.
+  if (h->zero || h->onebody || !h->real || h->P > kM)
+    return apply_fp64(h, psi, sigma, alpha, beta, st);
+  const fqegpu_graph_s* g = h->g;
+  const int64_t lena = g->a.len, lenb = g->b.len, N = lena * lenb;
+  if (lena > 65535) {
+    set_error("alpha string space of %lld exceeds the 65535 rows one launch covers",
+              (long long)lena);
+    return FQEGPU_ERR_UNSUPPORTED;
+  }
+  if (!h->oz) FQE_TRY(plan_create(h));
+  OzakiPlan* pl = h->oz;
+  const bool tri = h->compressed;
+  const int32_t* tabA = tri ? g->a.tab_tri : g->a.tab_full;
+  const int32_t* tabB = tri ? g->b.tab_tri : g->b.tab_full;
+  h->events_used = 0;
+  FQE_TRY(stage_mark(h, 0, 0, st));
+  k_oz_rowexp<<<(unsigned)lena, 256, 0, st>>>(lenb, psi, pl->d_rowexp);
+  k_oz_colexp_init<<<(unsigned)((lenb + 255) / 256), 256, 0, st>>>(lenb, pl->d_colexp);
+  {
+    const unsigned chunks = (unsigned)std::min<int64_t>(64, lena);
+    k_oz_colexp<<<dim3((unsigned)((lenb + 255) / 256), chunks), 256, 0, st>>>(
+        lena, lenb, psi, pl->d_colexp);
+  }
+  k_oz_globalexp<<<1, 256, 0, st>>>(lena, pl->d_rowexp, pl->d_misc);
+  k_oz_fixed<<<kNumSMs * 8, 256, 0, st>>>(N, psi, pl->d_misc, pl->d_psix);
+  FQE_CUDA(cudaGetLastError());
+  FQE_TRY(stage_mark(h, 0, 1, st));
+  OzArgs A;
+  A.P = pl->P;
+  A.KP = pl->KP;
+  A.lena = lena;
+  A.lenb = lenb;
+  A.nb = (int)((lenb + kDets - 1) / kDets);
+  A.ntiles = lena * (int64_t)A.nb;
+  A.tabA = tabA;
+  A.tabB = tabB;
+  A.psix = pl->d_psix;
+  A.rowexp = pl->d_rowexp;
+  A.colexp = pl->d_colexp;
+  A.misc = pl->d_misc;
+  A.vslices = pl->d_vslices;
+  A.vexp = pl->d_vexp;
+  A.G = pl->d_G;
+  A.err = pl->d_misc + 1;
+  const int grid = (int)std::min<int64_t>(pl->nsm, A.ntiles);
+  k_oz_contract<<<grid, kThreads, pl->smem, st>>>(A);
+  FQE_CUDA(cudaGetLastError());
+  FQE_TRY(stage_mark(h, 0, 2, st));
+  dim3 sg((unsigned)((lenb + 255) / 256), (unsigned)lena);
+  k_oz_scatter<<<sg, 256, 0, st>>>(pl->P, lena, lenb, tabA, tabB, pl->d_G, psi,
+                                   zmul_host(alpha, h->phase), beta, sigma);
+  FQE_CUDA(cudaGetLastError());
+  FQE_TRY(stage_mark(h, 0, 3, st));
+  int32_t errv = 0;
+  FQE_CUDA(cudaMemcpyAsync(&errv, pl->d_misc + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  FQE_CUDA(cudaStreamSynchronize(st));
+  if (errv != 0) {
+    set_error("tensor-core contraction: a bounded wait gave up (role %d)", errv);
+    return FQEGPU_ERR_TIMEOUT;
+  }
+  return FQEGPU_OK;
 }
+
 }  // namespace fqegpu

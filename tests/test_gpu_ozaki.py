@@ -1,0 +1,105 @@
+"""Tensor-core (tcgen05, Ozaki-split BF16) contraction: parity with the FP64
+path and the oracle.  Tolerance: relative 2-norm error <= 1e-10 (the stated
+target for the split form)."""
+
+import numpy
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_OZ = 1e-10
+
+
+def _rel(a, b):
+    return numpy.linalg.norm(a - b) / max(numpy.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture
+def ozaki(gpu):
+    from fqe_gb300 import settings
+    settings.precision = "ozaki"
+    yield gpu
+    settings.precision = "fp64"
+
+
+def _apply(gpu, norb, na, nb, h1, h2, psi):
+    d = gpu.FqeData(na, nb, norb)
+    d.set_wfn(strategy="from_data", raw_data=psi)
+    return d.apply((h1, h2)).to_numpy()
+
+
+@pytest.mark.parametrize("norb,na,nb", [(4, 2, 2), (6, 3, 2), (8, 4, 4), (9, 4, 3),
+                                        (10, 5, 5), (11, 3, 6), (12, 6, 6), (13, 6, 5)])
+def test_ozaki_matches_fp64_and_oracle(ozaki, oracle, norb, na, nb):
+    from fqe_gb300 import synthetic, settings
+    h1, h2, rng = synthetic.integrals(norb, norb + 4, 100 + norb)
+    g = oracle.graph(norb, na, nb)
+    psi = synthetic.wavefunction_coeff(g.lena, g.lenb, rng)
+    out = _apply(ozaki, norb, na, nb, h1, h2, psi)
+    settings.precision = "fp64"
+    ref64 = _apply(ozaki, norb, na, nb, h1, h2, psi)
+    settings.precision = "ozaki"
+    assert _rel(out, ref64) < TOL_OZ
+    if norb <= 10:
+        assert _rel(out, oracle.apply_spatial12(psi, h1, h2, g)) < TOL_OZ
+
+
+def test_ozaki_peaked_wavefunction(ozaki, oracle):
+    from fqe_gb300 import synthetic
+    norb, na, nb = 10, 5, 5
+    h1, h2, rng = synthetic.integrals(norb, 12, 5)
+    g = oracle.graph(norb, na, nb)
+    psi = 1e-6 * (rng.normal(size=(g.lena, g.lenb)) + 1j * rng.normal(size=(g.lena, g.lenb)))
+    psi[0, 0] = 0.99
+    psi[17, 3] = -0.1j
+    out = _apply(ozaki, norb, na, nb, h1, h2, psi)
+    assert _rel(out, oracle.apply_spatial12(psi, h1, h2, g)) < TOL_OZ
+
+
+def test_ozaki_imaginary_scale_and_e0(ozaki, oracle):
+    """-i t H (the Taylor operator) and e_0 ride through the same kernel."""
+    from fqe_gb300 import synthetic
+    norb, na, nb = 8, 4, 3
+    h1, h2, rng = synthetic.integrals(norb, 10, 9)
+    g = oracle.graph(norb, na, nb)
+    psi = synthetic.wavefunction_coeff(g.lena, g.lenb, rng)
+    out = _apply(ozaki, norb, na, nb, -0.05j * h1, -0.05j * h2, psi)
+    assert _rel(out, oracle.apply_spatial12(psi, -0.05j * h1, -0.05j * h2, g)) < TOL_OZ
+    wfn = ozaki.Wavefunction([[na + nb, na - nb, norb]])
+    wfn.set_wfn(strategy="from_data", raw_data={(na + nb, na - nb): psi})
+    res = wfn.apply(ozaki.get_restricted_hamiltonian((h1, h2), e_0=2.5))
+    ref = oracle.apply_restricted(psi, (h1, h2), 2.5, g)
+    assert _rel(res.get_coeff((na + nb, na - nb)).cpu().numpy(), ref) < TOL_OZ
+
+
+def test_ozaki_taylor(ozaki, oracle, golden):
+    gd = golden("taylor")
+    for key in [k for k in gd if k.startswith("out_")]:
+        tag = key[4:]
+        norb, na, nb = map(int, tag.split("_"))
+        wfn = ozaki.Wavefunction([[na + nb, na - nb, norb]])
+        wfn.set_wfn(strategy="from_data", raw_data={(na + nb, na - nb): gd["psi_" + tag]})
+        ham = ozaki.get_restricted_hamiltonian((gd["h1_" + tag], gd["h2_" + tag]))
+        out = wfn.apply_generated_unitary(float(gd["t_" + tag]), "taylor", ham,
+                                          accuracy=float(gd["acc_" + tag]))
+        assert _rel(out.get_coeff((na + nb, na - nb)).cpu().numpy(), gd[key]) < TOL_OZ
+
+
+def test_ozaki_complex_integrals_run_fp64_kernel(ozaki, oracle):
+    rng = numpy.random.default_rng(8)
+    norb, na, nb = 6, 3, 2
+    h1 = rng.normal(size=(norb,) * 2) + 1j * rng.normal(size=(norb,) * 2)
+    h2 = rng.normal(size=(norb,) * 4) + 1j * rng.normal(size=(norb,) * 4)
+    g = oracle.graph(norb, na, nb)
+    psi = rng.normal(size=(g.lena, g.lenb)) + 1j * rng.normal(size=(g.lena, g.lenb))
+    out = _apply(ozaki, norb, na, nb, h1, h2, psi)
+    assert _rel(out, oracle.apply_spatial12(psi, h1, h2, g)) < 1e-12
+
+
+def test_ozaki_deterministic(ozaki):
+    from fqe_gb300 import synthetic
+    h1, h2, rng = synthetic.integrals(10, 12, 3)
+    psi = synthetic.wavefunction_coeff(252, 210, rng)
+    a = _apply(ozaki, 10, 5, 4, h1, h2, psi)
+    b = _apply(ozaki, 10, 5, 4, h1, h2, psi)
+    assert numpy.array_equal(a, b)
