@@ -67,7 +67,6 @@ struct OzakiPlan {
   int32_t* d_vexp = nullptr;           // [128]
   longlong2* d_psix = nullptr;         // [N]
   int32_t* d_rowexp = nullptr;         // [lena]
-  int32_t* d_colexp = nullptr;         // [lenb]
   int32_t* d_misc = nullptr;           // [0] = global exponent, [1] = error
   float4* d_G = nullptr;               // [P][N]
   int nsm = 0;
@@ -81,8 +80,6 @@ struct OzArgs {
   const int32_t* tabA;
   const int32_t* tabB;
   const longlong2* psix;
-  const int32_t* rowexp;
-  const int32_t* colexp;
   const int32_t* misc;
   const __nv_bfloat16* vslices;
   const int32_t* vexp;
@@ -119,20 +116,16 @@ __device__ __forceinline__ void oz_abort(volatile int* abort_flag, int32_t* err,
   atomicExch(err, code);
 }
 
-__device__ __forceinline__ int det_exponent(const OzArgs& A, int64_t ia, int64_t ib) {
-  return max(A.rowexp[ia], A.colexp[ib]) + 1;
-}
-
-// 40-bit magnitude of x * 2^-sh (x fixed point), sign separate.
-__device__ __forceinline__ uint64_t mag40(long long x, int sh, uint32_t& neg) {
-  neg = x < 0 ? 1u : 0u;
-  uint64_t m = (uint64_t)(x < 0 ? -x : x);
-  if (sh >= 0) {
-    m = sh >= 64 ? 0ull : (m >> sh);
+// m * 2^-sh rounded to nearest, saturated to 40 bits (m < 2^63).
+__device__ __forceinline__ uint64_t round40(uint64_t m, int sh) {
+  uint64_t r;
+  if (sh > 0) {
+    r = sh >= 64 ? 0ull : ((m + (1ull << (sh - 1))) >> sh);
   } else {
-    m = (-sh >= 64) ? 0ull : (m << (-sh));
+    r = (-sh >= 40) ? 0ull : (m << (-sh));
   }
-  return m & ((1ull << 40) - 1ull);
+  const uint64_t cap = (1ull << 40) - 1ull;
+  return r > cap ? cap : r;
 }
 
 __device__ __forceinline__ uint32_t bf16_slice_pair(uint64_t m0, uint32_t n0,
@@ -144,7 +137,7 @@ __device__ __forceinline__ uint32_t bf16_slice_pair(uint64_t m0, uint32_t n0,
   return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-__global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
+__global__ void __maxnreg__(152) k_oz_contract(OzArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int KP = A.KP;
   const uint32_t v_elems = (uint32_t)kM * KP;
@@ -156,7 +149,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
   uint64_t* accfull = empty + kRing;
   uint64_t* accempty = accfull + 2;
   uint64_t* done = accempty + 2;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  uint64_t* ered = done + 1;  // [2] producer warps' column-exponent exchange
+  int32_t* eset = reinterpret_cast<int32_t*>(ered + 2);           // [2][kN]
+  uint8_t* red = reinterpret_cast<uint8_t*>(eset + 2 * kN);        // [2][8][kN]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(red + 2 * kProdWarps * kN);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -176,6 +172,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
       tc::mbar_init(&accempty[i], kEpiWarps);
     }
     tc::mbar_init(done, 1);
+    tc::mbar_init(&ered[0], kProdWarps);
+    tc::mbar_init(&ered[1], kProdWarps);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -238,6 +236,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
   } else if (warp < kEpiWarps) {
     const int p = tid;  // TMEM lane = pair row
     const int ev = (p < A.P) ? A.vexp[p] : 0;
+    const int g0 = A.misc[0];
     int64_t it = 0;
     for (int64_t t = blockIdx.x; t < A.ntiles; t += stride, ++it) {
       int64_t ia, ib0;
@@ -251,7 +250,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
       }
       tc::fence_after_sync();
       const uint32_t base = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(s * kAccCols);
-      const int rexp = A.rowexp[ia];
       for (int c0 = 0; c0 < kN; c0 += 16) {
         float va[16], vb[16], vc[16];
         tc::tmem_ld16(base + c0, va);
@@ -262,10 +260,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
         for (int j = 0; j < 16; j += 2) {
           const int64_t ib = ib0 + (c0 + j) / 2;
           if (ib >= A.lenb) continue;
-          const int sc = ev + max(rexp, A.colexp[ib]) + 1;
           float out[4];
 #pragma unroll
           for (int part = 0; part < 2; ++part) {
+            // column exponent: |D| < 2^(bits - 62 + g0)
+            const int sc = ev + eset[s * kN + c0 + j + part] - 62 + g0;
             const float x = va[j + part], y = vb[j + part], z = vc[j + part];
             // exact two-sum of the exact levels, then the rounded remainder
             const float h = x + y;
@@ -288,16 +287,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
   } else {
     const int pw = warp - (kEpiWarps + 1);  // 0..7
     const int noct = KP / 8;
-    const int g0 = A.misc[0];
     int64_t it = 0;
     for (int64_t t = blockIdx.x; t < A.ntiles; t += stride, ++it) {
       int64_t ia, ib0;
       tile_coords(A, t, ia, ib0);
       const int64_t ib = ib0 + lane;
       const bool valid = ib < A.lenb;
-      const int sh = valid ? 22 + det_exponent(A, ia, ib) - g0 : 0;
+      const int s = (int)(it & 1);
+      // gather D[q][det] for this lane's det and octets, as 62-bit fixed point
       uint64_t mre[2][8], mim[2][8];
       uint32_t nre[2], nim[2];
+      int blr = 0, bli = 0;
 #pragma unroll
       for (int oi = 0; oi < 2; ++oi) {
         nre[oi] = nim[oi] = 0u;
@@ -318,13 +318,48 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
               if (cb > 0) { re += x.x; im += x.y; } else { re -= x.x; im -= x.y; }
             }
           }
-          uint32_t n;
-          mre[oi][j] = mag40(re, sh, n);
-          nre[oi] |= n << j;
-          mim[oi][j] = mag40(im, sh, n);
-          nim[oi] |= n << j;
+          nre[oi] |= (re < 0 ? 1u : 0u) << j;
+          nim[oi] |= (im < 0 ? 1u : 0u) << j;
+          mre[oi][j] = (uint64_t)(re < 0 ? -re : re);
+          mim[oi][j] = (uint64_t)(im < 0 ? -im : im);
+          blr = max(blr, 64 - __clzll((long long)mre[oi][j]));
+          bli = max(bli, 64 - __clzll((long long)mim[oi][j]));
         }
       }
+      // exact exponent of each real column: maxima of the 8 warps' octets
+      red[(s * kProdWarps + pw) * kN + 2 * lane] = (uint8_t)blr;
+      red[(s * kProdWarps + pw) * kN + 2 * lane + 1] = (uint8_t)bli;
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&ered[s]);
+      if (!__all_sync(0xffffffffu, oz_wait(&ered[s], (uint32_t)((it >> 1) & 1), abort_flag))) {
+        if (lane == 0) oz_abort(abort_flag, A.err, 7);
+        break;
+      }
+      int br = 0, bi = 0;
+#pragma unroll
+      for (int w = 0; w < kProdWarps; ++w) {
+        br = max(br, (int)red[(s * kProdWarps + w) * kN + 2 * lane]);
+        bi = max(bi, (int)red[(s * kProdWarps + w) * kN + 2 * lane + 1]);
+      }
+      if (pw == 0) {
+        // the epilogue of the tile two back has finished with this set
+        if (!__all_sync(0xffffffffu, oz_wait(&accempty[s], (uint32_t)(((it >> 1) & 1) ^ 1),
+                                             abort_flag))) {
+          if (lane == 0) oz_abort(abort_flag, A.err, 8);
+          break;
+        }
+        eset[s * kN + 2 * lane] = br;
+        eset[s * kN + 2 * lane + 1] = bi;
+        __threadfence_block();
+      }
+      // 40-bit magnitudes relative to the column exponent, rounded to nearest
+#pragma unroll
+      for (int oi = 0; oi < 2; ++oi)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          mre[oi][j] = round40(mre[oi][j], br - 40);
+          mim[oi][j] = round40(mim[oi][j], bi - 40);
+        }
       bool ok = true;
       for (int b = 1; b <= kSlices; ++b) {
         const int64_t g = it * kSlices + (b - 1);
@@ -368,7 +403,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
   if (warp == kMmaWarp) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
-// ---- pre-pass: exponent bounds and the fixed-point copy of psi ------------
+// ---- pre-pass: global exponent and the fixed-point copy of psi ------------
 __device__ __forceinline__ int exp_of(double x) {
   // e with |x| < 2^e (frexp convention); kExpZero for 0
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -393,27 +428,6 @@ __global__ void k_oz_rowexp(int64_t lenb, const double2* __restrict__ psi,
     __syncthreads();
   }
   if (threadIdx.x == 0) rowexp[a] = red[0];
-}
-
-__global__ void k_oz_colexp_init(int64_t lenb, int32_t* __restrict__ colexp) {
-  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (b < lenb) colexp[b] = kExpZero;
-}
-
-// grid (column blocks, row chunks): each thread folds a chunk of rows of one
-// column, then one atomicMax per thread.
-__global__ void k_oz_colexp(int64_t lena, int64_t lenb, const double2* __restrict__ psi,
-                            int32_t* __restrict__ colexp) {
-  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (b >= lenb) return;
-  const int64_t chunk = (lena + gridDim.y - 1) / gridDim.y;
-  const int64_t a0 = blockIdx.y * chunk, a1 = min(lena, a0 + chunk);
-  int e = kExpZero;
-  for (int64_t a = a0; a < a1; ++a) {
-    const double2 v = psi[a * lenb + b];
-    e = max(e, max(exp_of(v.x), exp_of(v.y)));
-  }
-  atomicMax(&colexp[b], e);
 }
 
 __global__ void k_oz_globalexp(int64_t lena, const int32_t* __restrict__ rowexp,
@@ -524,8 +538,8 @@ static int plan_create(fqegpu_ham h) {
     vexp[p] = e;
     for (int q = 0; q < P; ++q) {
       const double v = h->vpair[(size_t)p * P + q];
-      const double y = std::floor(std::ldexp(std::fabs(v), 40 - e));
-      const uint64_t m = (uint64_t)y;
+      const double y = std::floor(std::ldexp(std::fabs(v), 40 - e) + 0.5);
+      const uint64_t m = std::min<uint64_t>((uint64_t)y, (1ull << 40) - 1ull);
       for (int k = 1; k <= kSlices; ++k) {
         const uint32_t byte = (uint32_t)((m >> (40 - 8 * k)) & 0xFFu);
         const float f = std::ldexp((float)byte, -8 * k) * (v < 0 ? -1.0f : 1.0f);
@@ -541,14 +555,14 @@ static int plan_create(fqegpu_ham h) {
   const int64_t lena = h->g->a.len, lenb = h->g->b.len, N = lena * lenb;
   FQE_CUDA(cudaMalloc(&pl->d_psix, sizeof(longlong2) * N));
   FQE_CUDA(cudaMalloc(&pl->d_rowexp, sizeof(int32_t) * lena));
-  FQE_CUDA(cudaMalloc(&pl->d_colexp, sizeof(int32_t) * lenb));
   FQE_CUDA(cudaMalloc(&pl->d_misc, sizeof(int32_t) * 4));
   FQE_CUDA(cudaMalloc(&pl->d_G, sizeof(float4) * (size_t)P * N));
   int dev = 0;
   FQE_CUDA(cudaGetDevice(&dev));
   FQE_CUDA(cudaDeviceGetAttribute(&pl->nsm, cudaDevAttrMultiProcessorCount, dev));
   pl->smem = sizeof(__nv_bfloat16) * ((size_t)kSlices * vel + (size_t)kRing * kN * KP) +
-             sizeof(uint64_t) * (2 * kRing + 5) + 16;
+             sizeof(uint64_t) * (2 * kRing + 7) + sizeof(int32_t) * 2 * kN +
+             2 * kProdWarps * kN + 16;
   FQE_CUDA(cudaFuncSetAttribute(k_oz_contract, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)pl->smem));
   return FQEGPU_OK;
@@ -561,7 +575,6 @@ void ozaki_destroy(fqegpu_ham h) {
   cudaFree(pl->d_vexp);
   cudaFree(pl->d_psix);
   cudaFree(pl->d_rowexp);
-  cudaFree(pl->d_colexp);
   cudaFree(pl->d_misc);
   cudaFree(pl->d_G);
   delete pl;
@@ -589,12 +602,6 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   h->events_used = 0;
   FQE_TRY(stage_mark(h, 0, 0, st));
   k_oz_rowexp<<<(unsigned)lena, 256, 0, st>>>(lenb, psi, pl->d_rowexp);
-  k_oz_colexp_init<<<(unsigned)((lenb + 255) / 256), 256, 0, st>>>(lenb, pl->d_colexp);
-  {
-    const unsigned chunks = (unsigned)std::min<int64_t>(64, lena);
-    k_oz_colexp<<<dim3((unsigned)((lenb + 255) / 256), chunks), 256, 0, st>>>(
-        lena, lenb, psi, pl->d_colexp);
-  }
   k_oz_globalexp<<<1, 256, 0, st>>>(lena, pl->d_rowexp, pl->d_misc);
   k_oz_fixed<<<kNumSMs * 8, 256, 0, st>>>(N, psi, pl->d_misc, pl->d_psix);
   FQE_CUDA(cudaGetLastError());
@@ -609,8 +616,6 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   A.tabA = tabA;
   A.tabB = tabB;
   A.psix = pl->d_psix;
-  A.rowexp = pl->d_rowexp;
-  A.colexp = pl->d_colexp;
   A.misc = pl->d_misc;
   A.vslices = pl->d_vslices;
   A.vexp = pl->d_vexp;
