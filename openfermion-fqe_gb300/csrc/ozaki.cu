@@ -137,7 +137,7 @@ __device__ __forceinline__ uint32_t bf16_slice_pair(uint64_t m0, uint32_t n0,
   return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-__global__ void __maxnreg__(152) k_oz_contract(OzArgs A) {
+__global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int KP = A.KP;
   const uint32_t v_elems = (uint32_t)kM * KP;
