@@ -31,6 +31,13 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 NORB, NALPHA, NBETA, NCHOL, SEED = 14, 7, 7, 28, 0
 METRIC = "H*psi det-updates/s at norb=14"
+
+
+def set_workload(norb, nalpha, nbeta, nchol):
+    """Other sector sizes, for profiling captures on a smaller case."""
+    global NORB, NALPHA, NBETA, NCHOL, METRIC
+    NORB, NALPHA, NBETA, NCHOL = norb, nalpha, nbeta, nchol
+    METRIC = f"H*psi det-updates/s at norb={norb}"
 UNIT = "det/s"
 
 
@@ -148,12 +155,12 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "restricted H*psi, norb=14 (7a,7b), 28 "
-                               "Cholesky vectors, seed 0", "norb": NORB,
+        "config": {"workload": f"restricted H*psi, norb={NORB} ({NALPHA}a,{NBETA}b), "
+                               f"{NCHOL} Cholesky vectors, seed {SEED}", "norb": NORB,
                    "nalpha": NALPHA, "nbeta": NBETA, "determinants": n},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores,
                          "kind": "port",
-                         "sample": "full norb=14 apply per step (the reference "
+                         "sample": f"full norb={NORB} apply per step (the reference "
                                    "C algorithm restated in oracle/fqe_oracle.c,"
                                    " OpenMP)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -310,7 +317,7 @@ def run_gpu(args):
         cores = os.cpu_count() or 1
         t_cpu = cpu_apply_time(h1, h2, psi_h, cores)
         cpu = {"value": n / t_cpu, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": "one full norb=14 apply of the oracle port "
+               "sample": f"one full norb={NORB} apply of the oracle port "
                          f"(reference C algorithm restated, OpenMP) took {t_cpu:.2f} s"}
 
     launches_per_apply = 3 * math.ceil(d.lenb() / max(1, _block_w(ham)))
@@ -320,8 +327,9 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if prec == "fp64" else "bf16-slices/f32-acc/f64",
         "data": "synthetic",
-        "config": {"workload": "restricted H*psi, norb=14 (7a,7b), 28 Cholesky "
-                               "vectors, seed 0", "norb": NORB, "nalpha": NALPHA,
+        "config": {"workload": f"restricted H*psi, norb={NORB} ({NALPHA}a,{NBETA}b), "
+                               f"{NCHOL} Cholesky vectors, seed {SEED}", "norb": NORB,
+                   "nalpha": NALPHA,
                    "nbeta": NBETA, "determinants": n, "precision": prec,
                    "pairs": P, "compressed_pairs": bool(ham.compressed),
                    "l2": "inputs larger than L2 (psi 188 MB; D and G blocks "
@@ -349,8 +357,9 @@ def _block_w(ham):
     from fqe_gb300 import _lib
     info = numpy.zeros(4, dtype=numpy.int64)
     _lib.call("fqegpu_ham_info", ham.handle, info.ctypes.data_as(ctypes.c_void_p))
-    per_col = 2 * info[0] * 3432 * 16
-    return int(info[3] // per_col) if info[3] else 3432
+    lena = math.comb(NORB, NALPHA)
+    per_col = 2 * info[0] * lena * 16
+    return int(info[3] // per_col) if info[3] else math.comb(NORB, NBETA)
 
 
 def main():
@@ -362,7 +371,17 @@ def main():
     ap.add_argument("--precision", choices=["auto", "fp64", "ozaki"],
                     default="auto")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--norb", type=int, default=14)
+    ap.add_argument("--nalpha", type=int, default=None)
+    ap.add_argument("--nbeta", type=int, default=None)
+    ap.add_argument("--nchol", type=int, default=None)
     args = ap.parse_args()
+    if args.norb != 14 or args.nalpha is not None or args.nbeta is not None:
+        na = args.nalpha if args.nalpha is not None else args.norb // 2
+        nb = args.nbeta if args.nbeta is not None else args.norb - args.norb // 2
+        from fqe_gb300 import synthetic
+        set_workload(args.norb, na, nb,
+                     args.nchol or synthetic.default_nchol(args.norb))
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

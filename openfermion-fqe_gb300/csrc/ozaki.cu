@@ -13,8 +13,10 @@
 // (byte * 2^{-8k}, exact in BF16), so every product lands on one absolute
 // scale and the products are grouped by level L = a + b into three TMEM
 // accumulators: L = 2 and L = 3 sum integers times 2^{-8L} below 2^24 and are
-// exact in FP32; L = 4..6 share one accumulator whose FP32 rounding sits
-// 2^-40 below the leading term.  Levels >= 7 are dropped (also ~2^-40).  The
+// exact in FP32; L = 4..7 share one accumulator whose FP32 rounding sits
+// 2^-40 below the leading term.  Levels >= 8 are dropped: 19 BF16 products
+// per tile (an emulation of this arithmetic gives ~1e-12 relative error on
+// G; stopping at level 6 gives ~1e-11).  The
 // three accumulators are combined into an FP32 pair (hi + lo, ~48 bits) and
 // scaled by 2^{eV(p) + E(I)}.
 //
@@ -46,6 +48,7 @@ namespace fqegpu {
 
 namespace {
 constexpr int kSlices = 5;
+constexpr int kMaxLevel = 7;   // pairs (a, b) with a + b <= 7 are contracted
 constexpr int kM = 128;        // MMA M (pairs, padded)
 constexpr int kN = 64;         // MMA N (real columns per tile)
 constexpr int kDets = 32;      // determinants per tile
@@ -114,6 +117,20 @@ __device__ __forceinline__ bool oz_wait(uint64_t* bar, uint32_t parity,
 __device__ __forceinline__ void oz_abort(volatile int* abort_flag, int32_t* err, int code) {
   *abort_flag = 1;
   atomicExch(err, code);
+}
+
+// 2^e as a float for -126 <= e <= 127.
+__device__ __forceinline__ float pow2f(int e) {
+  return __int_as_float((e + 127) << 23);
+}
+
+// x * 2^e in two exact steps (covers |e| <= 252; below that the result is
+// under FP32's range and flushes to zero).
+__device__ __forceinline__ float scale2(float x, int e) {
+  if (e < -252) return 0.0f;
+  e = min(e, 254);
+  const int e1 = e / 2, e2 = e - e1;
+  return (x * pow2f(e1)) * pow2f(e2);
 }
 
 // m * 2^-sh rounded to nearest, saturated to 40 bits (m < 2^63).
@@ -191,6 +208,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
       const uint32_t idesc = tc::make_idesc_bf16(kM, kN);
       const uint32_t sbo = (uint32_t)KP * 16u;
       const int ksteps = KP / 16;
+      // descriptors of k-step 0; k-step ks adds 256 bytes = 16 address units
+      uint64_t adesc0[kSlices];
+      for (int a = 0; a < kSlices; ++a)
+        adesc0[a] = tc::make_sdesc(tc::smem_u32(sV + (size_t)a * v_elems), 128, sbo);
+      uint64_t bdesc0[kRing];
+      for (int r = 0; r < kRing; ++r)
+        bdesc0[r] = tc::make_sdesc(tc::smem_u32(sD + (size_t)r * slot_elems), 128, sbo);
       int64_t it = 0;
       for (int64_t t = blockIdx.x; t < A.ntiles; t += stride, ++it) {
         const int s = (int)(it & 1);
@@ -211,16 +235,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
             break;
           }
           tc::fence_after_sync();
-          const uint32_t bbase = tc::smem_u32(sD + (size_t)slot * slot_elems);
-          for (int a = 1; a <= kSlices + 1 - b; ++a) {
+          const int amax = min(kSlices, kMaxLevel - b);
+          for (int a = 1; a <= amax; ++a) {
             const int lvl = a + b;
             const int ai = lvl == 2 ? 0 : (lvl == 3 ? 1 : 2);
             const uint32_t acc = acc0 + (uint32_t)(ai * kN);
-            const uint32_t abase = tc::smem_u32(sV + (size_t)(a - 1) * v_elems);
+            const uint64_t ad0 = adesc0[a - 1], bd0 = bdesc0[slot];
             for (int ks = 0; ks < ksteps; ++ks) {
-              const uint64_t ad = tc::make_sdesc(abase + ks * 256, 128, sbo);
-              const uint64_t bd = tc::make_sdesc(bbase + ks * 256, 128, sbo);
-              tc::mma_bf16(acc, ad, bd, idesc, (first[ai] && ks == 0) ? 0u : 1u);
+              tc::mma_bf16(acc, ad0 + (uint64_t)(16 * ks), bd0 + (uint64_t)(16 * ks), idesc,
+                           (first[ai] && ks == 0) ? 0u : 1u);
             }
             first[ai] = false;
           }
@@ -273,8 +296,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
             l += z;
             const float h2 = h + l;
             const float l2 = l - (h2 - h);
-            out[2 * part] = ldexpf(h2, sc);
-            out[2 * part + 1] = ldexpf(l2, sc);
+            out[2 * part] = scale2(h2, sc);
+            out[2 * part + 1] = scale2(l2, sc);
           }
           A.G[((int64_t)p * A.lena + ia) * A.lenb + ib] =
               make_float4(out[0], out[1], out[2], out[3]);
