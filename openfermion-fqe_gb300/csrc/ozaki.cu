@@ -11,13 +11,15 @@
 // (sign-magnitude bytes of 40-bit fixed-point values; eV(p) bounds row p of V,
 // E(I) bounds column I of D).  Every slice is stored as its true value
 // (byte * 2^{-8k}, exact in BF16), so every product lands on one absolute
-// scale and the products are grouped by level L = a + b into three TMEM
-// accumulators: L = 2 and L = 3 sum integers times 2^{-8L} below 2^24 and are
-// exact in FP32; L = 4..7 share one accumulator whose FP32 rounding sits
-// 2^-40 below the leading term.  Levels >= 8 are dropped: 19 BF16 products
-// per tile (an emulation of this arithmetic gives ~1e-12 relative error on
-// G; stopping at level 6 gives ~1e-11).  The
-// three accumulators are combined into an FP32 pair (hi + lo, ~48 bits) and
+// scale and the products are grouped by level L = a + b into four TMEM
+// accumulators: L = 2, 3 and 4 sum integers times 2^{-8L} that stay below
+// 2^24 (exact in FP32; level 4 can only exceed it for near-saturated bytes);
+// L = 5..7 share one accumulator whose FP32 rounding sits ~2^-48 below the
+// leading term even after ~100 accumulation steps.  Levels >= 8 are
+// dropped: 19 BF16 products per tile.  (Merging level 4 into the last
+// accumulator left ~1e-10 of accumulated rounding; stopping at level 6
+// leaves ~1e-11.)  The
+// four accumulators are combined into an FP32 pair (hi + lo, ~48 bits) and
 // scaled by 2^{eV(p) + E(I)}.
 //
 // D is never written to HBM: producer warps gather it from a 62-bit
@@ -58,7 +60,8 @@ constexpr int kEpiWarps = 4;
 constexpr int kMmaWarp = 4;
 constexpr int kProdWarps = 8;
 constexpr int kThreads = (kEpiWarps + 1 + kProdWarps) * 32;
-constexpr int kAccCols = 3 * kN;  // one accumulator set
+constexpr int kAccs = 4;           // levels 2, 3, 4 and 5..7
+constexpr int kAccCols = kAccs * kN;  // one accumulator set (two sets = 512)
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 constexpr int kExpZero = -2000;
@@ -145,11 +148,16 @@ __device__ __forceinline__ uint64_t round40(uint64_t m, int sh) {
   return r > cap ? cap : r;
 }
 
-__device__ __forceinline__ uint32_t bf16_slice_pair(uint64_t m0, uint32_t n0,
-                                                    uint64_t m1, uint32_t n1,
-                                                    int shift, float scale) {
-  const float f0 = (float)(uint32_t)((m0 >> shift) & 0xFFull) * (n0 ? -scale : scale);
-  const float f1 = (float)(uint32_t)((m1 >> shift) & 0xFFull) * (n1 ? -scale : scale);
+// Bytes k and k+1 of `w` as a bf16 pair (sign bits k, k+1 of `neg`), each
+// equal to +-byte * scale (exact: 8 significant bits, scale a power of two).
+// The byte becomes a float through the 2^23 magic constant.
+__device__ __forceinline__ uint32_t bf16_bytes_pair(uint32_t w, int k, uint32_t neg,
+                                                    float scale) {
+  const uint32_t b0 = (w >> (8 * k)) & 0xFFu, b1 = (w >> (8 * k + 8)) & 0xFFu;
+  const float f0 = (__uint_as_float(0x4B000000u | b0) - 8388608.0f) *
+                   (((neg >> k) & 1u) ? -scale : scale);
+  const float f1 = (__uint_as_float(0x4B000000u | b1) - 8388608.0f) *
+                   (((neg >> (k + 1)) & 1u) ? -scale : scale);
   const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
   return *reinterpret_cast<const uint32_t*>(&h);
 }
@@ -224,7 +232,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
         }
         tc::fence_after_sync();
         const uint32_t acc0 = tmem + (uint32_t)(s * kAccCols);
-        bool first[3] = {true, true, true};
+        bool first[kAccs] = {true, true, true, true};
         bool ok = true;
         for (int b = 1; b <= kSlices && ok; ++b) {
           const int64_t g = it * kSlices + (b - 1);
@@ -238,7 +246,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
           const int amax = min(kSlices, kMaxLevel - b);
           for (int a = 1; a <= amax; ++a) {
             const int lvl = a + b;
-            const int ai = lvl == 2 ? 0 : (lvl == 3 ? 1 : 2);
+            const int ai = lvl <= 4 ? lvl - 2 : 3;
             const uint32_t acc = acc0 + (uint32_t)(ai * kN);
             const uint64_t ad0 = adesc0[a - 1], bd0 = bdesc0[slot];
             for (int ks = 0; ks < ksteps; ++ks) {
@@ -274,10 +282,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
       tc::fence_after_sync();
       const uint32_t base = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(s * kAccCols);
       for (int c0 = 0; c0 < kN; c0 += 16) {
-        float va[16], vb[16], vc[16];
+        float va[16], vb[16], vc[16], vd[16];
         tc::tmem_ld16(base + c0, va);
         tc::tmem_ld16(base + kN + c0, vb);
         tc::tmem_ld16(base + 2 * kN + c0, vc);
+        tc::tmem_ld16(base + 3 * kN + c0, vd);
         if (p >= A.P) continue;
 #pragma unroll
         for (int j = 0; j < 16; j += 2) {
@@ -288,12 +297,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
           for (int part = 0; part < 2; ++part) {
             // column exponent: |D| < 2^(bits - 62 + g0)
             const int sc = ev + eset[s * kN + c0 + j + part] - 62 + g0;
-            const float x = va[j + part], y = vb[j + part], z = vc[j + part];
-            // exact two-sum of the exact levels, then the rounded remainder
+            const float x = va[j + part], y = vb[j + part];
+            // exact two-sum of levels 2 and 3, then levels 4 and 5..7
             const float h = x + y;
             const float bb = h - x;
             float l = (x - (h - bb)) + (y - bb);
-            l += z;
+            l += vc[j + part];
+            l += vd[j + part];
             const float h2 = h + l;
             const float l2 = l - (h2 - h);
             out[2 * part] = scale2(h2, sc);
@@ -375,15 +385,29 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
         eset[s * kN + 2 * lane + 1] = bi;
         __threadfence_block();
       }
-      // 40-bit magnitudes relative to the column exponent, rounded to nearest
+      // 40-bit magnitudes relative to the column exponent, rounded to nearest;
+      // the five slice bytes of each value are packed four to a register:
+      // pk[oi][part][2 (b-1) + h] holds byte b of q = 8 o + 4 h .. 8 o + 4 h + 3
+      uint32_t pk[2][2][2 * kSlices];
 #pragma unroll
       for (int oi = 0; oi < 2; ++oi)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          mre[oi][j] = round40(mre[oi][j], br - 40);
-          mim[oi][j] = round40(mim[oi][j], bi - 40);
+        for (int part = 0; part < 2; ++part) {
+          const int e = (part ? bi : br) - 40;
+#pragma unroll
+          for (int w = 0; w < 2 * kSlices; ++w) pk[oi][part][w] = 0u;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const uint64_t m = round40(part ? mim[oi][j] : mre[oi][j], e);
+#pragma unroll
+            for (int b = 1; b <= kSlices; ++b) {
+              const uint32_t byte = (uint32_t)(m >> (40 - 8 * b)) & 0xFFu;
+              pk[oi][part][2 * (b - 1) + (j >> 2)] |= byte << (8 * (j & 3));
+            }
+          }
         }
       bool ok = true;
+#pragma unroll
       for (int b = 1; b <= kSlices; ++b) {
         const int64_t g = it * kSlices + (b - 1);
         const int slot = (int)(g % kRing);
@@ -395,21 +419,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
           break;
         }
         __nv_bfloat16* sb = sD + (size_t)slot * slot_elems;
-        const int shift = 40 - 8 * b;
-        const float scale = ldexpf(1.0f, -8 * b);
+        const float scale = pow2f(-8 * b);
 #pragma unroll
         for (int oi = 0; oi < 2; ++oi) {
           const int o = pw + 8 * oi;
           if (o >= noct) continue;
 #pragma unroll
           for (int part = 0; part < 2; ++part) {
-            const uint64_t* m = part ? mim[oi] : mre[oi];
             const uint32_t nb = part ? nim[oi] : nre[oi];
+            const uint32_t lo = pk[oi][part][2 * (b - 1)], hi = pk[oi][part][2 * (b - 1) + 1];
             uint4 v;
-            v.x = bf16_slice_pair(m[0], nb & 1u, m[1], (nb >> 1) & 1u, shift, scale);
-            v.y = bf16_slice_pair(m[2], (nb >> 2) & 1u, m[3], (nb >> 3) & 1u, shift, scale);
-            v.z = bf16_slice_pair(m[4], (nb >> 4) & 1u, m[5], (nb >> 5) & 1u, shift, scale);
-            v.w = bf16_slice_pair(m[6], (nb >> 6) & 1u, m[7], (nb >> 7) & 1u, shift, scale);
+            v.x = bf16_bytes_pair(lo, 0, nb, scale);
+            v.y = bf16_bytes_pair(lo, 2, nb, scale);
+            v.z = bf16_bytes_pair(hi, 0, nb >> 4, scale);
+            v.w = bf16_bytes_pair(hi, 2, nb >> 4, scale);
             *reinterpret_cast<uint4*>(sb + tc::kmajor_offset(2 * lane + part, 8 * o, KP)) = v;
           }
         }
