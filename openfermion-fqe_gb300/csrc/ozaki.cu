@@ -148,18 +148,56 @@ __device__ __forceinline__ uint64_t round40(uint64_t m, int sh) {
   return r > cap ? cap : r;
 }
 
-// Bytes k and k+1 of `w` as a bf16 pair (sign bits k, k+1 of `neg`), each
-// equal to +-byte * scale (exact: 8 significant bits, scale a power of two).
-// The byte becomes a float through the 2^23 magic constant.
+// D[q][det] (real and imaginary part) in 62-bit fixed point: the alpha and
+// beta sources of the pair q through the target tables.
+__device__ __forceinline__ void gather_d(const OzArgs& A, int q, bool live, uint32_t ia,
+                                         uint32_t ib, uint32_t lena, uint32_t lenb,
+                                         long long& re, long long& im) {
+  re = 0;
+  im = 0;
+  if (!live || q >= A.P) return;
+  const int32_t ca = __ldg(A.tabA + (uint32_t)q * lena + ia);
+  const int32_t cb = __ldg(A.tabB + (uint32_t)q * lenb + ib);
+  if (ca) {
+    const longlong2 x = __ldg(A.psix + ((uint32_t)(abs(ca) - 1) * lenb + ib));
+    if (ca > 0) { re += x.x; im += x.y; } else { re -= x.x; im -= x.y; }
+  }
+  if (cb) {
+    const longlong2 x = __ldg(A.psix + (ia * lenb + (uint32_t)(abs(cb) - 1)));
+    if (cb > 0) { re += x.x; im += x.y; } else { re -= x.x; im -= x.y; }
+  }
+}
+
+// Inserts the five slice bytes of the 40-bit magnitude m (value j of 8) into
+// the packed words: word 2 (b - 1) + j / 4, byte j % 4 holds slice b.
+__device__ __forceinline__ void pack_slices(uint32_t (&pk)[2 * kSlices], uint64_t m, int j) {
+  const uint32_t lo = (uint32_t)m, hi = (uint32_t)(m >> 32);
+  const int h = j >> 2, pos = j & 3;
+  // selector: keep bytes of pk (0..3) except `pos`, which takes byte `src` of
+  // the second operand (4..7)
+  auto sel = [pos](int src) -> uint32_t {
+    uint32_t r = 0x3210u;
+    r &= ~(0xFu << (4 * pos));
+    r |= (uint32_t)(4 + src) << (4 * pos);
+    return r;
+  };
+  pk[0 + h] = __byte_perm(pk[0 + h], hi, sel(0));  // slice 1: bits 32..39
+  pk[2 + h] = __byte_perm(pk[2 + h], lo, sel(3));  // slice 2: bits 24..31
+  pk[4 + h] = __byte_perm(pk[4 + h], lo, sel(2));  // slice 3
+  pk[6 + h] = __byte_perm(pk[6 + h], lo, sel(1));  // slice 4
+  pk[8 + h] = __byte_perm(pk[8 + h], lo, sel(0));  // slice 5: bits 0..7
+}
+
+// Bytes k and k+1 of `w` as a bf16 pair, signs from bits 0 and 1 of `neg`,
+// each +-byte * 2^-8b (exact); `ebits` are the float bits of 2^(23 - 8b).
 __device__ __forceinline__ uint32_t bf16_bytes_pair(uint32_t w, int k, uint32_t neg,
-                                                    float scale) {
-  const uint32_t b0 = (w >> (8 * k)) & 0xFFu, b1 = (w >> (8 * k + 8)) & 0xFFu;
-  const float f0 = (__uint_as_float(0x4B000000u | b0) - 8388608.0f) *
-                   (((neg >> k) & 1u) ? -scale : scale);
-  const float f1 = (__uint_as_float(0x4B000000u | b1) - 8388608.0f) *
-                   (((neg >> (k + 1)) & 1u) ? -scale : scale);
+                                                    uint32_t ebits) {
+  const float off = __uint_as_float(ebits);
+  const float f0 = __uint_as_float(__byte_perm(w, ebits, 0x7650u + (uint32_t)k)) - off;
+  const float f1 = __uint_as_float(__byte_perm(w, ebits, 0x7650u + (uint32_t)k + 1u)) - off;
   const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
-  return *reinterpret_cast<const uint32_t*>(&h);
+  const uint32_t sgn = ((neg & 1u) << 15) | (((neg >> 1) & 1u) << 31);
+  return *reinterpret_cast<const uint32_t*>(&h) ^ sgn;
 }
 
 __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
@@ -306,8 +344,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
             l += vd[j + part];
             const float h2 = h + l;
             const float l2 = l - (h2 - h);
-            out[2 * part] = scale2(h2, sc);
-            out[2 * part + 1] = scale2(l2, sc);
+            if (sc >= -126 && sc <= 127) {
+              const float f = pow2f(sc);
+              out[2 * part] = h2 * f;
+              out[2 * part + 1] = l2 * f;
+            } else {
+              out[2 * part] = scale2(h2, sc);
+              out[2 * part + 1] = scale2(l2, sc);
+            }
           }
           A.G[((int64_t)p * A.lena + ia) * A.lenb + ib] =
               make_float4(out[0], out[1], out[2], out[3]);
@@ -320,46 +364,29 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
   } else {
     const int pw = warp - (kEpiWarps + 1);  // 0..7
     const int noct = KP / 8;
+    const uint32_t lena32 = (uint32_t)A.lena, lenb32 = (uint32_t)A.lenb;
     int64_t it = 0;
     for (int64_t t = blockIdx.x; t < A.ntiles; t += stride, ++it) {
-      int64_t ia, ib0;
-      tile_coords(A, t, ia, ib0);
-      const int64_t ib = ib0 + lane;
-      const bool valid = ib < A.lenb;
+      int64_t ia64, ib064;
+      tile_coords(A, t, ia64, ib064);
+      const uint32_t ia = (uint32_t)ia64, ib = (uint32_t)ib064 + lane;
+      const bool valid = ib < lenb32;
       const int s = (int)(it & 1);
-      // gather D[q][det] for this lane's det and octets, as 62-bit fixed point
-      uint64_t mre[2][8], mim[2][8];
-      uint32_t nre[2], nim[2];
+      // pass 1: exact exponent of each real column (bit length of the
+      // largest fixed-point |D|), no values kept
       int blr = 0, bli = 0;
 #pragma unroll
       for (int oi = 0; oi < 2; ++oi) {
-        nre[oi] = nim[oi] = 0u;
         const int o = pw + 8 * oi;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          long long re = 0, im = 0;
-          const int q = 8 * o + j;
-          if (o < noct && valid && q < A.P) {
-            const int32_t ca = A.tabA[(int64_t)q * A.lena + ia];
-            const int32_t cb = A.tabB[(int64_t)q * A.lenb + ib];
-            if (ca) {
-              const longlong2 x = A.psix[(int64_t)(abs(ca) - 1) * A.lenb + ib];
-              if (ca > 0) { re += x.x; im += x.y; } else { re -= x.x; im -= x.y; }
-            }
-            if (cb) {
-              const longlong2 x = A.psix[ia * A.lenb + (abs(cb) - 1)];
-              if (cb > 0) { re += x.x; im += x.y; } else { re -= x.x; im -= x.y; }
-            }
-          }
-          nre[oi] |= (re < 0 ? 1u : 0u) << j;
-          nim[oi] |= (im < 0 ? 1u : 0u) << j;
-          mre[oi][j] = (uint64_t)(re < 0 ? -re : re);
-          mim[oi][j] = (uint64_t)(im < 0 ? -im : im);
-          blr = max(blr, 64 - __clzll((long long)mre[oi][j]));
-          bli = max(bli, 64 - __clzll((long long)mim[oi][j]));
+          long long re, im;
+          gather_d(A, 8 * o + j, o < noct && valid, ia, ib, lena32, lenb32, re, im);
+          blr = max(blr, 64 - __clzll(re < 0 ? -re : re));
+          bli = max(bli, 64 - __clzll(im < 0 ? -im : im));
         }
       }
-      // exact exponent of each real column: maxima of the 8 warps' octets
+      // the 8 warps' partial maxima meet through an mbarrier
       red[(s * kProdWarps + pw) * kN + 2 * lane] = (uint8_t)blr;
       red[(s * kProdWarps + pw) * kN + 2 * lane + 1] = (uint8_t)bli;
       __syncwarp();
@@ -385,27 +412,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
         eset[s * kN + 2 * lane + 1] = bi;
         __threadfence_block();
       }
-      // 40-bit magnitudes relative to the column exponent, rounded to nearest;
-      // the five slice bytes of each value are packed four to a register:
-      // pk[oi][part][2 (b-1) + h] holds byte b of q = 8 o + 4 h .. 8 o + 4 h + 3
+      // pass 2: gather again (L1/L2 resident), round to 40 bits relative to
+      // the column exponent and pack the five slice bytes of each value, four
+      // values to a register: pk[oi][part][2 (b-1) + h] holds byte b of
+      // q = 8 o + 4 h .. 8 o + 4 h + 3
       uint32_t pk[2][2][2 * kSlices];
+      uint32_t nre[2], nim[2];
 #pragma unroll
-      for (int oi = 0; oi < 2; ++oi)
+      for (int oi = 0; oi < 2; ++oi) {
+        const int o = pw + 8 * oi;
+        nre[oi] = nim[oi] = 0u;
 #pragma unroll
-        for (int part = 0; part < 2; ++part) {
-          const int e = (part ? bi : br) - 40;
+        for (int w = 0; w < 2 * kSlices; ++w) pk[oi][0][w] = pk[oi][1][w] = 0u;
 #pragma unroll
-          for (int w = 0; w < 2 * kSlices; ++w) pk[oi][part][w] = 0u;
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const uint64_t m = round40(part ? mim[oi][j] : mre[oi][j], e);
-#pragma unroll
-            for (int b = 1; b <= kSlices; ++b) {
-              const uint32_t byte = (uint32_t)(m >> (40 - 8 * b)) & 0xFFu;
-              pk[oi][part][2 * (b - 1) + (j >> 2)] |= byte << (8 * (j & 3));
-            }
-          }
+        for (int j = 0; j < 8; ++j) {
+          long long re, im;
+          gather_d(A, 8 * o + j, o < noct && valid, ia, ib, lena32, lenb32, re, im);
+          nre[oi] |= (re < 0 ? 1u : 0u) << j;
+          nim[oi] |= (im < 0 ? 1u : 0u) << j;
+          pack_slices(pk[oi][0], round40((uint64_t)(re < 0 ? -re : re), br - 40), j);
+          pack_slices(pk[oi][1], round40((uint64_t)(im < 0 ? -im : im), bi - 40), j);
         }
+      }
       bool ok = true;
 #pragma unroll
       for (int b = 1; b <= kSlices; ++b) {
@@ -419,7 +447,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
           break;
         }
         __nv_bfloat16* sb = sD + (size_t)slot * slot_elems;
-        const float scale = pow2f(-8 * b);
+        // float bits of 2^(23 - 8b): OR-ing a byte into the mantissa and
+        // subtracting 2^(23 - 8b) gives byte * 2^-8b exactly
+        const uint32_t ebits = (uint32_t)(150 - 8 * b) << 23;
 #pragma unroll
         for (int oi = 0; oi < 2; ++oi) {
           const int o = pw + 8 * oi;
@@ -429,10 +459,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
             const uint32_t nb = part ? nim[oi] : nre[oi];
             const uint32_t lo = pk[oi][part][2 * (b - 1)], hi = pk[oi][part][2 * (b - 1) + 1];
             uint4 v;
-            v.x = bf16_bytes_pair(lo, 0, nb, scale);
-            v.y = bf16_bytes_pair(lo, 2, nb, scale);
-            v.z = bf16_bytes_pair(hi, 0, nb >> 4, scale);
-            v.w = bf16_bytes_pair(hi, 2, nb >> 4, scale);
+            v.x = bf16_bytes_pair(lo, 0, nb, ebits);
+            v.y = bf16_bytes_pair(lo, 2, nb >> 2, ebits);
+            v.z = bf16_bytes_pair(hi, 0, nb >> 4, ebits);
+            v.w = bf16_bytes_pair(hi, 2, nb >> 6, ebits);
             *reinterpret_cast<uint4*>(sb + tc::kmajor_offset(2 * lane + part, 8 * o, KP)) = v;
           }
         }
