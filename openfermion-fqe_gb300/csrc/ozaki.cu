@@ -75,6 +75,7 @@ struct OzakiPlan {
   int32_t* d_rowexp = nullptr;         // [lena]
   int32_t* d_misc = nullptr;           // [0] = global exponent, [1] = error
   float4* d_G = nullptr;               // [P][N]
+  uchar2* d_bexp = nullptr;            // [N]
   int nsm = 0;
   size_t smem = 0;
 };
@@ -89,6 +90,7 @@ struct OzArgs {
   const int32_t* misc;
   const __nv_bfloat16* vslices;
   const int32_t* vexp;
+  uchar2* bexp;  // [N] bit length of max |D| (fixed point), re / im
   float4* G;
   int32_t* err;
 };
@@ -212,10 +214,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
   uint64_t* accfull = empty + kRing;
   uint64_t* accempty = accfull + 2;
   uint64_t* done = accempty + 2;
-  uint64_t* ered = done + 1;  // [2] producer warps' column-exponent exchange
-  int32_t* eset = reinterpret_cast<int32_t*>(ered + 2);           // [2][kN]
-  uint8_t* red = reinterpret_cast<uint8_t*>(eset + 2 * kN);        // [2][8][kN]
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(red + 2 * kProdWarps * kN);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -235,8 +234,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
       tc::mbar_init(&accempty[i], kEpiWarps);
     }
     tc::mbar_init(done, 1);
-    tc::mbar_init(&ered[0], kProdWarps);
-    tc::mbar_init(&ered[1], kProdWarps);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -247,7 +244,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  const int64_t stride = gridDim.x;
+  // each CTA owns a contiguous run of tiles (consecutive tiles share an alpha
+  // row, so its beta sources stay cache resident)
+  const int64_t t_begin = A.ntiles * blockIdx.x / gridDim.x;
+  const int64_t t_end = A.ntiles * (blockIdx.x + 1) / gridDim.x;
 
   if (warp == kMmaWarp) {
     if (lane == 0) {
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
       for (int r = 0; r < kRing; ++r)
         bdesc0[r] = tc::make_sdesc(tc::smem_u32(sD + (size_t)r * slot_elems), 128, sbo);
       int64_t it = 0;
-      for (int64_t t = blockIdx.x; t < A.ntiles; t += stride, ++it) {
+      for (int64_t t = t_begin; t < t_end; ++t, ++it) {
         const int s = (int)(it & 1);
         if (!oz_wait(&accempty[s], (uint32_t)(((it >> 1) & 1) ^ 1), abort_flag)) {
           oz_abort(abort_flag, A.err, 2);
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
     const int ev = (p < A.P) ? A.vexp[p] : 0;
     const int g0 = A.misc[0];
     int64_t it = 0;
-    for (int64_t t = blockIdx.x; t < A.ntiles; t += stride, ++it) {
+    for (int64_t t = t_begin; t < t_end; ++t, ++it) {
       int64_t ia, ib0;
       tile_coords(A, t, ia, ib0);
       const int s = (int)(it & 1);
@@ -334,7 +334,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
 #pragma unroll
           for (int part = 0; part < 2; ++part) {
             // column exponent: |D| < 2^(bits - 62 + g0)
-            const int sc = ev + eset[s * kN + c0 + j + part] - 62 + g0;
+            const uchar2 be = A.bexp[ia * A.lenb + ib];
+            const int sc = ev + (int)(part ? be.y : be.x) - 62 + g0;
             const float x = va[j + part], y = vb[j + part];
             // exact two-sum of levels 2 and 3, then levels 4 and 5..7
             const float h = x + y;
@@ -366,54 +367,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
     const int noct = KP / 8;
     const uint32_t lena32 = (uint32_t)A.lena, lenb32 = (uint32_t)A.lenb;
     int64_t it = 0;
-    for (int64_t t = blockIdx.x; t < A.ntiles; t += stride, ++it) {
+    for (int64_t t = t_begin; t < t_end; ++t, ++it) {
       int64_t ia64, ib064;
       tile_coords(A, t, ia64, ib064);
       const uint32_t ia = (uint32_t)ia64, ib = (uint32_t)ib064 + lane;
       const bool valid = ib < lenb32;
-      const int s = (int)(it & 1);
-      // pass 1: exact exponent of each real column (bit length of the
-      // largest fixed-point |D|), no values kept
-      int blr = 0, bli = 0;
-#pragma unroll
-      for (int oi = 0; oi < 2; ++oi) {
-        const int o = pw + 8 * oi;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          long long re, im;
-          gather_d(A, 8 * o + j, o < noct && valid, ia, ib, lena32, lenb32, re, im);
-          blr = max(blr, 64 - __clzll(re < 0 ? -re : re));
-          bli = max(bli, 64 - __clzll(im < 0 ? -im : im));
-        }
-      }
-      // the 8 warps' partial maxima meet through an mbarrier
-      red[(s * kProdWarps + pw) * kN + 2 * lane] = (uint8_t)blr;
-      red[(s * kProdWarps + pw) * kN + 2 * lane + 1] = (uint8_t)bli;
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&ered[s]);
-      if (!__all_sync(0xffffffffu, oz_wait(&ered[s], (uint32_t)((it >> 1) & 1), abort_flag))) {
-        if (lane == 0) oz_abort(abort_flag, A.err, 7);
-        break;
-      }
-      int br = 0, bi = 0;
-#pragma unroll
-      for (int w = 0; w < kProdWarps; ++w) {
-        br = max(br, (int)red[(s * kProdWarps + w) * kN + 2 * lane]);
-        bi = max(bi, (int)red[(s * kProdWarps + w) * kN + 2 * lane + 1]);
-      }
-      if (pw == 0) {
-        // the epilogue of the tile two back has finished with this set
-        if (!__all_sync(0xffffffffu, oz_wait(&accempty[s], (uint32_t)(((it >> 1) & 1) ^ 1),
-                                             abort_flag))) {
-          if (lane == 0) oz_abort(abort_flag, A.err, 8);
-          break;
-        }
-        eset[s * kN + 2 * lane] = br;
-        eset[s * kN + 2 * lane + 1] = bi;
-        __threadfence_block();
-      }
-      // pass 2: gather again (L1/L2 resident), round to 40 bits relative to
-      // the column exponent and pack the five slice bytes of each value, four
+      // exact exponents of this lane's real columns (pre-pass k_oz_bexp)
+      const uchar2 be = valid ? A.bexp[ia * lenb32 + ib] : make_uchar2(0, 0);
+      const int br = be.x, bi = be.y;
+      // gather, round to 40 bits relative to the column exponent and pack
+      // the five slice bytes of each value, four
       // values to a register: pk[oi][part][2 (b-1) + h] holds byte b of
       // q = 8 o + 4 h .. 8 o + 4 h + 3
       uint32_t pk[2][2][2 * kSlices];
@@ -486,6 +449,25 @@ __device__ __forceinline__ int exp_of(double x) {
   const int be = (int)((b >> 52) & 0x7FF);
   if (be == 0) return (b << 1) == 0 ? kExpZero : -1022;  // subnormals: bound
   return be - 1022;
+}
+
+// Exact exponent of every real column of D: the bit length of the largest
+// fixed-point |D[q][I]| over the pairs q, for the real and imaginary part.
+// A plain gather with full occupancy, so the contraction's producer needs a
+// single pass.
+__global__ void __launch_bounds__(256) k_oz_bexp(OzArgs A) {
+  const uint32_t ia = blockIdx.y;
+  const uint32_t ib = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lena = (uint32_t)A.lena, lenb = (uint32_t)A.lenb;
+  if (ib >= lenb) return;
+  int br = 0, bi = 0;
+  for (int q = 0; q < A.P; ++q) {
+    long long re, im;
+    gather_d(A, q, true, ia, ib, lena, lenb, re, im);
+    br = max(br, 64 - __clzll(re < 0 ? -re : re));
+    bi = max(bi, 64 - __clzll(im < 0 ? -im : im));
+  }
+  A.bexp[ia * lenb + ib] = make_uchar2((unsigned char)br, (unsigned char)bi);
 }
 
 __global__ void k_oz_rowexp(int64_t lenb, const double2* __restrict__ psi,
@@ -633,12 +615,12 @@ static int plan_create(fqegpu_ham h) {
   FQE_CUDA(cudaMalloc(&pl->d_rowexp, sizeof(int32_t) * lena));
   FQE_CUDA(cudaMalloc(&pl->d_misc, sizeof(int32_t) * 4));
   FQE_CUDA(cudaMalloc(&pl->d_G, sizeof(float4) * (size_t)P * N));
+  FQE_CUDA(cudaMalloc(&pl->d_bexp, sizeof(uchar2) * N));
   int dev = 0;
   FQE_CUDA(cudaGetDevice(&dev));
   FQE_CUDA(cudaDeviceGetAttribute(&pl->nsm, cudaDevAttrMultiProcessorCount, dev));
   pl->smem = sizeof(__nv_bfloat16) * ((size_t)kSlices * vel + (size_t)kRing * kN * KP) +
-             sizeof(uint64_t) * (2 * kRing + 7) + sizeof(int32_t) * 2 * kN +
-             2 * kProdWarps * kN + 16;
+             sizeof(uint64_t) * (2 * kRing + 5) + 16;
   FQE_CUDA(cudaFuncSetAttribute(k_oz_contract, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)pl->smem));
   return FQEGPU_OK;
@@ -653,6 +635,7 @@ void ozaki_destroy(fqegpu_ham h) {
   cudaFree(pl->d_rowexp);
   cudaFree(pl->d_misc);
   cudaFree(pl->d_G);
+  cudaFree(pl->d_bexp);
   delete pl;
   h->oz = nullptr;
 }
@@ -681,7 +664,6 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   k_oz_globalexp<<<1, 256, 0, st>>>(lena, pl->d_rowexp, pl->d_misc);
   k_oz_fixed<<<kNumSMs * 8, 256, 0, st>>>(N, psi, pl->d_misc, pl->d_psix);
   FQE_CUDA(cudaGetLastError());
-  FQE_TRY(stage_mark(h, 0, 1, st));
   OzArgs A;
   A.P = pl->P;
   A.KP = pl->KP;
@@ -696,7 +678,11 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   A.vslices = pl->d_vslices;
   A.vexp = pl->d_vexp;
   A.G = pl->d_G;
+  A.bexp = pl->d_bexp;
   A.err = pl->d_misc + 1;
+  k_oz_bexp<<<dim3((unsigned)((lenb + 255) / 256), (unsigned)lena), 256, 0, st>>>(A);
+  FQE_CUDA(cudaGetLastError());
+  FQE_TRY(stage_mark(h, 0, 1, st));
   const int grid = (int)std::min<int64_t>(pl->nsm, A.ntiles);
   k_oz_contract<<<grid, kThreads, pl->smem, st>>>(A);
   FQE_CUDA(cudaGetLastError());
