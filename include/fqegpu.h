@@ -130,6 +130,23 @@ int fqegpu_apply_host(fqegpu_ham h, const double *h_psi, double *h_sigma,
                       double alpha_re, double alpha_im, double beta_re,
                       double beta_im, int precision);
 
+/* The same FP64 apply without any device allocation.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory while they run —
+ * a program whose device memory belongs to another allocator (a framework's
+ * caching allocator, a fixed arena) or a loop that cannot afford the device
+ * synchronisation cudaMalloc/cudaFree imply.  All working memory (string
+ * tables, pair matrix, D/G blocks) comes from one static 64 MiB device array
+ * that every GPU loading the library holds until exit; sectors whose tables
+ * plus one beta column exceed it return FQEGPU_ERR_UNSUPPORTED.  The first
+ * call on a device looks up the array's address (make it before any stream
+ * capture).  Calls share the array: calls that overlap on the GPU race and
+ * must be serialised by the caller.  Synchronous: returns after sigma is
+ * written.  h_h1 may be NULL; h_h2 is required. */
+int fqegpu_apply_noalloc(int norb, int nalpha, int nbeta, const double *h_h1,
+                         const double *h_h2, const double *d_psi,
+                         double *d_sigma, double alpha_re, double alpha_im,
+                         double beta_re, double beta_im, void *stream);
+
 /* ---- A7: dvec ------------------------------------------------------------
  * d_dvec[i][j][a][b] = sum_J <I|E_ij|J> psi_J   (zdvec_make,
  * lib/fqe_data.c:350-377, FqeData.calculate_dvec_spatial fqe_data.py:2149)

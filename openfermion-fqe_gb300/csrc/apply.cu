@@ -658,3 +658,24 @@ extern "C" int fqegpu_ham_stage_ms(fqegpu_ham h, double* h_ms3) {
     }
   return FQEGPU_OK;
 }
+
+namespace fqegpu {
+// Launchers of the FP64 pair contraction and of sigma = beta psi for callers
+// that provide their own device memory.
+int launch_pairgemm(int P, int64_t ncol, const double* Vr, const double2* Vc,
+                    const double2* D, double2* G, cudaStream_t st) {
+  dim3 grid((unsigned)((ncol + 63) / 64), (unsigned)((P + 63) / 64));
+  if (Vc)
+    k_pairgemm_f64<true><<<grid, 256, 0, st>>>(P, ncol, nullptr, Vc, D, G);
+  else
+    k_pairgemm_f64<false><<<grid, 256, 0, st>>>(P, ncol, Vr, nullptr, D, G);
+  FQE_CUDA(cudaGetLastError());
+  return FQEGPU_OK;
+}
+
+int launch_axpby(int64_t n, double2 beta, const double2* x, double2* y, cudaStream_t st) {
+  k_axpby<<<grid_1d(n), 256, 0, st>>>(n, beta, x, y);
+  FQE_CUDA(cudaGetLastError());
+  return FQEGPU_OK;
+}
+}  // namespace fqegpu

@@ -369,3 +369,39 @@ extern "C" int fqegpu_graph_maps(fqegpu_graph g, int spin, int32_t* h_out) {
   }
   return FQEGPU_OK;
 }
+
+namespace fqegpu {
+// Builds the tables of one spin into caller-provided device memory (`mem`,
+// `bytes`) with the same kernels as fqegpu_graph_create; returns the number
+// of bytes used, or -1 when they do not fit.
+int64_t build_spin_into(int norb, int nele, void* mem, size_t bytes, cudaStream_t st,
+                        SpinTables& t) {
+  t.nele = nele;
+  t.len = binom_host(norb, nele);
+  t.ndexc = nele * (norb - nele + 1);
+  const int64_t len = t.len;
+  const int P = norb * norb, PT = norb * (norb + 1) / 2;
+  auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t s_str = up(sizeof(uint64_t) * len);
+  const size_t s_z = up(sizeof(int32_t) * (size_t)(nele * norb > 0 ? nele * norb : 1));
+  const size_t s_dexc = up(sizeof(int32_t) * 3 * (size_t)(len * t.ndexc > 0 ? len * t.ndexc : 1));
+  const size_t s_full = up(sizeof(int32_t) * (size_t)(P > 0 ? P : 1) * len);
+  const size_t s_tri = up(sizeof(int32_t) * (size_t)(PT > 0 ? PT : 1) * len);
+  const size_t need = s_str + s_z + s_dexc + s_full + s_tri;
+  if (need > bytes) return -1;
+  unsigned char* p = static_cast<unsigned char*>(mem);
+  t.strings = reinterpret_cast<uint64_t*>(p);
+  t.zmat = reinterpret_cast<int32_t*>(p + s_str);
+  t.dexc = reinterpret_cast<int32_t*>(p + s_str + s_z);
+  t.tab_full = reinterpret_cast<int32_t*>(p + s_str + s_z + s_dexc);
+  t.tab_tri = reinterpret_cast<int32_t*>(p + s_str + s_z + s_dexc + s_full);
+  if (cudaMemsetAsync(t.tab_full, 0, s_full + s_tri, st) != cudaSuccess) return -1;
+  if (nele * norb > 0) k_zmatrix<<<(nele * norb + 127) / 128, 128, 0, st>>>(norb, nele, t.zmat);
+  k_strings<<<(unsigned)((len + 255) / 256), 256, 0, st>>>(norb, nele, len, t.zmat, t.strings);
+  if (t.ndexc > 0)
+    k_dexc<<<(unsigned)((len + 127) / 128), 128, 0, st>>>(norb, len, t.ndexc, t.strings, t.zmat,
+                                                          t.dexc, t.tab_full, t.tab_tri);
+  if (cudaGetLastError() != cudaSuccess) return -1;
+  return (int64_t)need;
+}
+}  // namespace fqegpu

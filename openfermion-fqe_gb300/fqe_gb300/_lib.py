@@ -49,6 +49,7 @@ _SIGNATURES = {
     "fqegpu_ham_stage_ms": [_P, _P],
     "fqegpu_apply": [_P, _P, _P, _D, _D, _D, _D, _I, _P],
     "fqegpu_apply_host": [_P, _P, _P, _D, _D, _D, _D, _I],
+    "fqegpu_apply_noalloc": [_I, _I, _I, _P, _P, _P, _P, _D, _D, _D, _D, _P],
     "fqegpu_make_dvec": [_P, _P, _P, _P],
     "fqegpu_make_coeff": [_P, _P, _P, _I, _P],
     "fqegpu_diagonal_coulomb": [_P, _P, _P, _P, _I, _P],
