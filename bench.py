@@ -279,8 +279,17 @@ def run_gpu(args):
     flops_fp64_peak = 1.10  # TFLOP/s, GB300 DGEMM probed with torch on this machine
     # algorithmic work per apply (contraction 2 real GEMMs of
     # P x P x N; gather writes and scatter reads D/G at 16 B per element)
-    contract_flops = 2.0 * 2.0 * P * P * n
-    gather_bytes = 16.0 * n + 16.0 * P * n
+    KP = (P + 15) // 16 * 16
+    if prec == "ozaki":
+        # slicing kernel writes 5 BF16 slices of 64 x KP per 32-det tile;
+        # contraction: 19 useful BF16 products of P x P x (2 real columns)
+        ntiles = d.lena() * ((d.lenb() + 31) // 32)
+        slice_bytes = ntiles * 5 * 64 * KP * 2.0
+        contract_flops = 19 * 2.0 * P * P * 2.0 * n
+        gather_bytes = 16.0 * n + slice_bytes + 2.0 * n
+    else:
+        contract_flops = 2.0 * 2.0 * P * P * n
+        gather_bytes = 16.0 * n + 16.0 * P * n
     scatter_bytes = 16.0 * P * n + 16.0 * n
     names = ["gather", "contraction", "scatter"]
     dom = int(numpy.argmax(stage))
@@ -320,7 +329,10 @@ def run_gpu(args):
                "sample": f"one full norb={NORB} apply of the oracle port "
                          f"(reference C algorithm restated, OpenMP) took {t_cpu:.2f} s"}
 
-    launches_per_apply = 3 * math.ceil(d.lenb() / max(1, _block_w(ham)))
+    if prec == "ozaki":
+        launches_per_apply = 6  # rowexp, globalexp, fixed, slice, mma, scatter
+    else:
+        launches_per_apply = 3 * math.ceil(d.lenb() / max(1, _block_w(ham)))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max,

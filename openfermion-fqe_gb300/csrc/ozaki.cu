@@ -54,12 +54,12 @@ constexpr int kMaxLevel = 7;   // pairs (a, b) with a + b <= 7 are contracted
 constexpr int kM = 128;        // MMA M (pairs, padded)
 constexpr int kN = 64;         // MMA N (real columns per tile)
 constexpr int kDets = 32;      // determinants per tile
-constexpr int kRing = 4;       // D-slice ring depth
-constexpr int kSuperBlocks = 32;
+constexpr int kMaxRing = 8;    // slice-chunk ring depth (fits shared memory)
 constexpr int kEpiWarps = 4;
 constexpr int kMmaWarp = 4;
-constexpr int kProdWarps = 8;
-constexpr int kThreads = (kEpiWarps + 1 + kProdWarps) * 32;
+constexpr int kLoadWarp = 5;
+constexpr int kThreads = 6 * 32;
+constexpr int kSliceThreads = 256;  // one CTA of k_oz_slice = one tile
 constexpr int kAccs = 4;           // levels 2, 3, 4 and 5..7
 constexpr int kAccCols = kAccs * kN;  // one accumulator set (two sets = 512)
 constexpr uint32_t kTmemCols = 512;
@@ -76,12 +76,14 @@ struct OzakiPlan {
   int32_t* d_misc = nullptr;           // [0] = global exponent, [1] = error
   float4* d_G = nullptr;               // [P][N]
   uchar2* d_bexp = nullptr;            // [N]
+  __nv_bfloat16* d_dslices = nullptr;  // [ntiles][5][64 * KP] smem images
+  int ring = 0;
   int nsm = 0;
   size_t smem = 0;
 };
 
 struct OzArgs {
-  int P, KP;
+  int P, KP, ring;
   int64_t lena, lenb, ntiles;
   int nb;  // column blocks per row
   const int32_t* tabA;
@@ -91,19 +93,16 @@ struct OzArgs {
   const __nv_bfloat16* vslices;
   const int32_t* vexp;
   uchar2* bexp;  // [N] bit length of max |D| (fixed point), re / im
+  __nv_bfloat16* dslices;  // [ntiles][5][64 * KP]
   float4* G;
   int32_t* err;
 };
 
-// Tile t -> (alpha row, first beta column) with column super-blocks.
+// Tile t -> (alpha row, first beta column): row-major, 32 determinants.
 __device__ __forceinline__ void tile_coords(const OzArgs& A, int64_t t, int64_t& ia,
                                             int64_t& ib0) {
-  const int64_t per_sb = A.lena * kSuperBlocks;
-  const int64_t s = t / per_sb;
-  const int64_t r = t - s * per_sb;
-  const int64_t ws = min((int64_t)kSuperBlocks, (int64_t)A.nb - s * kSuperBlocks);
-  ia = r / ws;
-  ib0 = (s * kSuperBlocks + (r - ia * ws)) * kDets;
+  ia = t / A.nb;
+  ib0 = (t - ia * A.nb) * kDets;
 }
 
 // Bounded wait that also gives up when another role has aborted.
@@ -202,16 +201,98 @@ __device__ __forceinline__ uint32_t bf16_bytes_pair(uint32_t w, int k, uint32_t 
   return *reinterpret_cast<const uint32_t*>(&h) ^ sgn;
 }
 
-__global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
+// ---- slicing: D tiles in the tensor core's shared-memory image ------------
+// One CTA per tile of 32 determinants; warp w owns determinants 4w..4w+3 (MMA
+// rows 8w..8w+7), lane l the determinant 4w + (l & 3) and octets l >> 2 and
+// (l >> 2) + 8 of the pair index.  Writes, per tile and slice, the 64 x KP
+// BF16 operand in the canonical K-major core-matrix layout (a warp stores
+// 1 KB contiguous per instruction pair), and the exact exponent of every real
+// column (shuffle maximum over the lanes of a determinant).
+__global__ void __launch_bounds__(kSliceThreads) k_oz_slice(OzArgs A) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t t = blockIdx.x;
+  int64_t ia64, ib064;
+  tile_coords(A, t, ia64, ib064);
+  const uint32_t lena32 = (uint32_t)A.lena, lenb32 = (uint32_t)A.lenb;
+  const uint32_t ia = (uint32_t)ia64;
+  const int d = 4 * w + (lane & 3);
+  const uint32_t ib = (uint32_t)ib064 + d;
+  const bool valid = ib < lenb32;
+  const int KP = A.KP, noct = KP / 8;
+  const int oct[2] = {lane >> 2, (lane >> 2) + 8};
+  uint64_t mre[2][8], mim[2][8];
+  uint32_t nre[2] = {0u, 0u}, nim[2] = {0u, 0u};
+  int blr = 0, bli = 0;
+#pragma unroll
+  for (int oi = 0; oi < 2; ++oi)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      long long re, im;
+      gather_d(A, 8 * oct[oi] + j, oct[oi] < noct && valid, ia, ib, lena32, lenb32, re, im);
+      nre[oi] |= (re < 0 ? 1u : 0u) << j;
+      nim[oi] |= (im < 0 ? 1u : 0u) << j;
+      mre[oi][j] = (uint64_t)(re < 0 ? -re : re);
+      mim[oi][j] = (uint64_t)(im < 0 ? -im : im);
+      blr = max(blr, 64 - __clzll((long long)mre[oi][j]));
+      bli = max(bli, 64 - __clzll((long long)mim[oi][j]));
+    }
+#pragma unroll
+  for (int m = 4; m < 32; m <<= 1) {
+    blr = max(blr, __shfl_xor_sync(0xffffffffu, blr, m));
+    bli = max(bli, __shfl_xor_sync(0xffffffffu, bli, m));
+  }
+  if (lane < 4 && valid)
+    A.bexp[ia * lenb32 + ib] = make_uchar2((unsigned char)blr, (unsigned char)bli);
+  uint32_t pk[2][2][2 * kSlices];
+#pragma unroll
+  for (int oi = 0; oi < 2; ++oi) {
+#pragma unroll
+    for (int x = 0; x < 2 * kSlices; ++x) pk[oi][0][x] = pk[oi][1][x] = 0u;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      pack_slices(pk[oi][0], round40(mre[oi][j], blr - 40), j);
+      pack_slices(pk[oi][1], round40(mim[oi][j], bli - 40), j);
+    }
+  }
+  const size_t chunk = (size_t)kN * KP;
+  __nv_bfloat16* out = A.dslices + (size_t)t * kSlices * chunk;
+#pragma unroll
+  for (int b = 1; b <= kSlices; ++b) {
+    const uint32_t ebits = (uint32_t)(150 - 8 * b) << 23;
+    __nv_bfloat16* dst = out + (size_t)(b - 1) * chunk;
+#pragma unroll
+    for (int oi = 0; oi < 2; ++oi) {
+      if (oct[oi] >= noct) continue;
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+        const uint32_t nb = part ? nim[oi] : nre[oi];
+        const uint32_t lo = pk[oi][part][2 * (b - 1)], hi = pk[oi][part][2 * (b - 1) + 1];
+        uint4 v;
+        v.x = bf16_bytes_pair(lo, 0, nb, ebits);
+        v.y = bf16_bytes_pair(lo, 2, nb >> 2, ebits);
+        v.z = bf16_bytes_pair(hi, 0, nb >> 4, ebits);
+        v.w = bf16_bytes_pair(hi, 2, nb >> 6, ebits);
+        *reinterpret_cast<uint4*>(dst + tc::kmajor_offset(2 * d + part, 8 * oct[oi], KP)) = v;
+      }
+    }
+  }
+}
+
+// ---- contraction: bulk-copied slices, tcgen05 MMAs, TMEM epilogue -----------
+// Persistent, one CTA per SM, 6 warps: warps 0-3 epilogue, warp 4 TMEM
+// allocation + MMA issue (lane 0), warp 5 lane 0 streams the slice images of
+// each tile into a ring of shared-memory slots with cp.async.bulk.
+__global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  const int KP = A.KP;
+  const int KP = A.KP, R = A.ring;
   const uint32_t v_elems = (uint32_t)kM * KP;
   const uint32_t slot_elems = (uint32_t)kN * KP;
+  const uint32_t slot_bytes = slot_elems * 2u;
   __nv_bfloat16* sV = reinterpret_cast<__nv_bfloat16*>(smem);
   __nv_bfloat16* sD = sV + kSlices * v_elems;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sD + kRing * slot_elems);
-  uint64_t* empty = full + kRing;
-  uint64_t* accfull = empty + kRing;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sD + (size_t)R * slot_elems);
+  uint64_t* empty = full + kMaxRing;
+  uint64_t* accfull = empty + kMaxRing;
   uint64_t* accempty = accfull + 2;
   uint64_t* done = accempty + 2;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
@@ -225,8 +306,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
     for (int i = tid; i < n16; i += blockDim.x) dst[i] = src[i];
   }
   if (tid == 0) {
-    for (int i = 0; i < kRing; ++i) {
-      tc::mbar_init(&full[i], kProdWarps);
+    for (int i = 0; i < R; ++i) {
+      tc::mbar_init(&full[i], 1);
       tc::mbar_init(&empty[i], 1);
     }
     for (int i = 0; i < 2; ++i) {
@@ -245,11 +326,32 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
   // each CTA owns a contiguous run of tiles (consecutive tiles share an alpha
-  // row, so its beta sources stay cache resident)
+  // row, so the G rows it writes are contiguous too)
   const int64_t t_begin = A.ntiles * blockIdx.x / gridDim.x;
   const int64_t t_end = A.ntiles * (blockIdx.x + 1) / gridDim.x;
 
-  if (warp == kMmaWarp) {
+  if (warp == kLoadWarp) {
+    if (lane == 0) {
+      int64_t it = 0;
+      for (int64_t t = t_begin; t < t_end; ++t, ++it) {
+        const __nv_bfloat16* src = A.dslices + (size_t)t * kSlices * slot_elems;
+        bool ok = true;
+        for (int b = 0; b < kSlices; ++b) {
+          const int64_t g = it * kSlices + b;
+          const int slot = (int)(g % R);
+          if (!oz_wait(&empty[slot], (uint32_t)(((g / R) & 1) ^ 1), abort_flag)) {
+            oz_abort(abort_flag, A.err, 5);
+            ok = false;
+            break;
+          }
+          tc::mbar_arrive_expect_tx(&full[slot], slot_bytes);
+          tc::bulk_g2s(sD + (size_t)slot * slot_elems, src + (size_t)b * slot_elems,
+                       slot_bytes, &full[slot]);
+        }
+        if (!ok) break;
+      }
+    }
+  } else if (warp == kMmaWarp) {
     if (lane == 0) {
       const uint32_t idesc = tc::make_idesc_bf16(kM, kN);
       const uint32_t sbo = (uint32_t)KP * 16u;
@@ -258,9 +360,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
       uint64_t adesc0[kSlices];
       for (int a = 0; a < kSlices; ++a)
         adesc0[a] = tc::make_sdesc(tc::smem_u32(sV + (size_t)a * v_elems), 128, sbo);
-      uint64_t bdesc0[kRing];
-      for (int r = 0; r < kRing; ++r)
-        bdesc0[r] = tc::make_sdesc(tc::smem_u32(sD + (size_t)r * slot_elems), 128, sbo);
       int64_t it = 0;
       for (int64_t t = t_begin; t < t_end; ++t, ++it) {
         const int s = (int)(it & 1);
@@ -274,19 +373,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
         bool ok = true;
         for (int b = 1; b <= kSlices && ok; ++b) {
           const int64_t g = it * kSlices + (b - 1);
-          const int slot = (int)(g % kRing);
-          if (!oz_wait(&full[slot], (uint32_t)((g / kRing) & 1), abort_flag)) {
+          const int slot = (int)(g % R);
+          if (!oz_wait(&full[slot], (uint32_t)((g / R) & 1), abort_flag)) {
             oz_abort(abort_flag, A.err, 3);
             ok = false;
             break;
           }
           tc::fence_after_sync();
+          const uint64_t bd0 =
+              tc::make_sdesc(tc::smem_u32(sD + (size_t)slot * slot_elems), 128, sbo);
           const int amax = min(kSlices, kMaxLevel - b);
           for (int a = 1; a <= amax; ++a) {
             const int lvl = a + b;
             const int ai = lvl <= 4 ? lvl - 2 : 3;
             const uint32_t acc = acc0 + (uint32_t)(ai * kN);
-            const uint64_t ad0 = adesc0[a - 1], bd0 = bdesc0[slot];
+            const uint64_t ad0 = adesc0[a - 1];
             for (int ks = 0; ks < ksteps; ++ks) {
               tc::mma_bf16(acc, ad0 + (uint64_t)(16 * ks), bd0 + (uint64_t)(16 * ks), idesc,
                            (first[ai] && ks == 0) ? 0u : 1u);
@@ -302,7 +403,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
       tc::mma_commit(done);
       if (!oz_wait(done, 0, abort_flag) && !*abort_flag) oz_abort(abort_flag, A.err, 6);
     }
-  } else if (warp < kEpiWarps) {
+  } else {
     const int p = tid;  // TMEM lane = pair row
     const int ev = (p < A.P) ? A.vexp[p] : 0;
     const int g0 = A.misc[0];
@@ -330,11 +431,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
         for (int j = 0; j < 16; j += 2) {
           const int64_t ib = ib0 + (c0 + j) / 2;
           if (ib >= A.lenb) continue;
+          const uchar2 be = A.bexp[ia * A.lenb + ib];
           float out[4];
 #pragma unroll
           for (int part = 0; part < 2; ++part) {
             // column exponent: |D| < 2^(bits - 62 + g0)
-            const uchar2 be = A.bexp[ia * A.lenb + ib];
             const int sc = ev + (int)(part ? be.y : be.x) - 62 + g0;
             const float x = va[j + part], y = vb[j + part];
             // exact two-sum of levels 2 and 3, then levels 4 and 5..7
@@ -362,79 +463,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_contract(OzArgs A) {
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&accempty[s]);
     }
-  } else {
-    const int pw = warp - (kEpiWarps + 1);  // 0..7
-    const int noct = KP / 8;
-    const uint32_t lena32 = (uint32_t)A.lena, lenb32 = (uint32_t)A.lenb;
-    int64_t it = 0;
-    for (int64_t t = t_begin; t < t_end; ++t, ++it) {
-      int64_t ia64, ib064;
-      tile_coords(A, t, ia64, ib064);
-      const uint32_t ia = (uint32_t)ia64, ib = (uint32_t)ib064 + lane;
-      const bool valid = ib < lenb32;
-      // exact exponents of this lane's real columns (pre-pass k_oz_bexp)
-      const uchar2 be = valid ? A.bexp[ia * lenb32 + ib] : make_uchar2(0, 0);
-      const int br = be.x, bi = be.y;
-      // gather, round to 40 bits relative to the column exponent and pack
-      // the five slice bytes of each value, four
-      // values to a register: pk[oi][part][2 (b-1) + h] holds byte b of
-      // q = 8 o + 4 h .. 8 o + 4 h + 3
-      uint32_t pk[2][2][2 * kSlices];
-      uint32_t nre[2], nim[2];
-#pragma unroll
-      for (int oi = 0; oi < 2; ++oi) {
-        const int o = pw + 8 * oi;
-        nre[oi] = nim[oi] = 0u;
-#pragma unroll
-        for (int w = 0; w < 2 * kSlices; ++w) pk[oi][0][w] = pk[oi][1][w] = 0u;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          long long re, im;
-          gather_d(A, 8 * o + j, o < noct && valid, ia, ib, lena32, lenb32, re, im);
-          nre[oi] |= (re < 0 ? 1u : 0u) << j;
-          nim[oi] |= (im < 0 ? 1u : 0u) << j;
-          pack_slices(pk[oi][0], round40((uint64_t)(re < 0 ? -re : re), br - 40), j);
-          pack_slices(pk[oi][1], round40((uint64_t)(im < 0 ? -im : im), bi - 40), j);
-        }
-      }
-      bool ok = true;
-#pragma unroll
-      for (int b = 1; b <= kSlices; ++b) {
-        const int64_t g = it * kSlices + (b - 1);
-        const int slot = (int)(g % kRing);
-        const bool got = __all_sync(
-            0xffffffffu, oz_wait(&empty[slot], (uint32_t)(((g / kRing) & 1) ^ 1), abort_flag));
-        if (!got) {
-          if (lane == 0) oz_abort(abort_flag, A.err, 5);
-          ok = false;
-          break;
-        }
-        __nv_bfloat16* sb = sD + (size_t)slot * slot_elems;
-        // float bits of 2^(23 - 8b): OR-ing a byte into the mantissa and
-        // subtracting 2^(23 - 8b) gives byte * 2^-8b exactly
-        const uint32_t ebits = (uint32_t)(150 - 8 * b) << 23;
-#pragma unroll
-        for (int oi = 0; oi < 2; ++oi) {
-          const int o = pw + 8 * oi;
-          if (o >= noct) continue;
-#pragma unroll
-          for (int part = 0; part < 2; ++part) {
-            const uint32_t nb = part ? nim[oi] : nre[oi];
-            const uint32_t lo = pk[oi][part][2 * (b - 1)], hi = pk[oi][part][2 * (b - 1) + 1];
-            uint4 v;
-            v.x = bf16_bytes_pair(lo, 0, nb, ebits);
-            v.y = bf16_bytes_pair(lo, 2, nb >> 2, ebits);
-            v.z = bf16_bytes_pair(hi, 0, nb >> 4, ebits);
-            v.w = bf16_bytes_pair(hi, 2, nb >> 6, ebits);
-            *reinterpret_cast<uint4*>(sb + tc::kmajor_offset(2 * lane + part, 8 * o, KP)) = v;
-          }
-        }
-        tc::fence_proxy_async_smem();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&full[slot]);
-      }
-      if (!ok) break;
-    }
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -449,25 +477,6 @@ __device__ __forceinline__ int exp_of(double x) {
   const int be = (int)((b >> 52) & 0x7FF);
   if (be == 0) return (b << 1) == 0 ? kExpZero : -1022;  // subnormals: bound
   return be - 1022;
-}
-
-// Exact exponent of every real column of D: the bit length of the largest
-// fixed-point |D[q][I]| over the pairs q, for the real and imaginary part.
-// A plain gather with full occupancy, so the contraction's producer needs a
-// single pass.
-__global__ void __launch_bounds__(256) k_oz_bexp(OzArgs A) {
-  const uint32_t ia = blockIdx.y;
-  const uint32_t ib = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t lena = (uint32_t)A.lena, lenb = (uint32_t)A.lenb;
-  if (ib >= lenb) return;
-  int br = 0, bi = 0;
-  for (int q = 0; q < A.P; ++q) {
-    long long re, im;
-    gather_d(A, q, true, ia, ib, lena, lenb, re, im);
-    br = max(br, 64 - __clzll(re < 0 ? -re : re));
-    bi = max(bi, 64 - __clzll(im < 0 ? -im : im));
-  }
-  A.bexp[ia * lenb + ib] = make_uchar2((unsigned char)br, (unsigned char)bi);
 }
 
 __global__ void k_oz_rowexp(int64_t lenb, const double2* __restrict__ psi,
@@ -616,12 +625,25 @@ static int plan_create(fqegpu_ham h) {
   FQE_CUDA(cudaMalloc(&pl->d_misc, sizeof(int32_t) * 4));
   FQE_CUDA(cudaMalloc(&pl->d_G, sizeof(float4) * (size_t)P * N));
   FQE_CUDA(cudaMalloc(&pl->d_bexp, sizeof(uchar2) * N));
+  const int64_t ntiles = lena * ((lenb + kDets - 1) / kDets);
+  FQE_CUDA(cudaMalloc(&pl->d_dslices,
+                      sizeof(__nv_bfloat16) * (size_t)ntiles * kSlices * kN * KP));
   int dev = 0;
   FQE_CUDA(cudaGetDevice(&dev));
   FQE_CUDA(cudaDeviceGetAttribute(&pl->nsm, cudaDevAttrMultiProcessorCount, dev));
-  pl->smem = sizeof(__nv_bfloat16) * ((size_t)kSlices * vel + (size_t)kRing * kN * KP) +
-             sizeof(uint64_t) * (2 * kRing + 5) + 16;
-  FQE_CUDA(cudaFuncSetAttribute(k_oz_contract, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  // as many slice slots as shared memory holds after the V slices
+  int smax = 0;
+  FQE_CUDA(cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t fixed = sizeof(__nv_bfloat16) * (size_t)kSlices * vel +
+                       sizeof(uint64_t) * (2 * kMaxRing + 5) + 16;
+  const size_t slot = sizeof(__nv_bfloat16) * (size_t)kN * KP;
+  pl->ring = (int)std::min<size_t>(kMaxRing, ((size_t)smax - fixed) / slot);
+  if (pl->ring < 2) {
+    set_error("shared memory too small for the tensor-core contraction");
+    return FQEGPU_ERR_UNSUPPORTED;
+  }
+  pl->smem = fixed + (size_t)pl->ring * slot;
+  FQE_CUDA(cudaFuncSetAttribute(k_oz_mma, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)pl->smem));
   return FQEGPU_OK;
 }
@@ -636,6 +658,7 @@ void ozaki_destroy(fqegpu_ham h) {
   cudaFree(pl->d_misc);
   cudaFree(pl->d_G);
   cudaFree(pl->d_bexp);
+  cudaFree(pl->d_dslices);
   delete pl;
   h->oz = nullptr;
 }
@@ -667,6 +690,7 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   OzArgs A;
   A.P = pl->P;
   A.KP = pl->KP;
+  A.ring = pl->ring;
   A.lena = lena;
   A.lenb = lenb;
   A.nb = (int)((lenb + kDets - 1) / kDets);
@@ -679,12 +703,13 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   A.vexp = pl->d_vexp;
   A.G = pl->d_G;
   A.bexp = pl->d_bexp;
+  A.dslices = pl->d_dslices;
   A.err = pl->d_misc + 1;
-  k_oz_bexp<<<dim3((unsigned)((lenb + 255) / 256), (unsigned)lena), 256, 0, st>>>(A);
+  k_oz_slice<<<(unsigned)A.ntiles, kSliceThreads, 0, st>>>(A);
   FQE_CUDA(cudaGetLastError());
   FQE_TRY(stage_mark(h, 0, 1, st));
   const int grid = (int)std::min<int64_t>(pl->nsm, A.ntiles);
-  k_oz_contract<<<grid, kThreads, pl->smem, st>>>(A);
+  k_oz_mma<<<grid, kThreads, pl->smem, st>>>(A);
   FQE_CUDA(cudaGetLastError());
   FQE_TRY(stage_mark(h, 0, 2, st));
   dim3 sg((unsigned)((lenb + 255) / 256), (unsigned)lena);
