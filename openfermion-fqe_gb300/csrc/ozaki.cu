@@ -59,7 +59,7 @@ constexpr int kEpiWarps = 4;
 constexpr int kMmaWarp = 4;
 constexpr int kLoadWarp = 5;
 constexpr int kThreads = 6 * 32;
-constexpr int kSliceThreads = 256;  // one CTA of k_oz_slice = one tile
+constexpr int kSliceThreads = 512;  // one CTA of k_oz_slice = one tile
 constexpr int kAccs = 4;           // levels 2, 3, 4 and 5..7
 constexpr int kAccCols = kAccs * kN;  // one accumulator set (two sets = 512)
 constexpr uint32_t kTmemCols = 512;
@@ -202,58 +202,64 @@ __device__ __forceinline__ uint32_t bf16_bytes_pair(uint32_t w, int k, uint32_t 
 }
 
 // ---- slicing: D tiles in the tensor core's shared-memory image ------------
-// One CTA per tile of 32 determinants; warp w owns determinants 4w..4w+3 (MMA
-// rows 8w..8w+7), lane l the determinant 4w + (l & 3) and octets l >> 2 and
-// (l >> 2) + 8 of the pair index.  Writes, per tile and slice, the 64 x KP
-// BF16 operand in the canonical K-major core-matrix layout (a warp stores
-// 1 KB contiguous per instruction pair), and the exact exponent of every real
-// column (shuffle maximum over the lanes of a determinant).
-__global__ void __launch_bounds__(kSliceThreads) k_oz_slice(OzArgs A) {
+// One CTA (16 warps) per tile of 32 determinants.  Warp w owns determinants
+// 4 (w % 8) .. 4 (w % 8) + 3 (MMA rows 8 (w % 8) .. + 7) and octets
+// 8 (w / 8) .. 8 (w / 8) + 7 of the pair index; lane l the determinant
+// 4 (w % 8) + (l & 3) and the octet 8 (w / 8) + (l >> 2).  Writes, per tile and
+// slice, the 64 x KP BF16 operand in the canonical K-major core-matrix layout
+// (a warp stores 1 KB contiguous per instruction pair) and the exact exponent
+// of every real column (shuffle maximum inside a warp, shared memory across
+// the two warps of a determinant group).
+__global__ void __launch_bounds__(kSliceThreads, 2) k_oz_slice(OzArgs A) {
+  __shared__ int red[16][4];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int grp = w & 7, half = w >> 3;
   const int64_t t = blockIdx.x;
   int64_t ia64, ib064;
   tile_coords(A, t, ia64, ib064);
   const uint32_t lena32 = (uint32_t)A.lena, lenb32 = (uint32_t)A.lenb;
   const uint32_t ia = (uint32_t)ia64;
-  const int d = 4 * w + (lane & 3);
+  const int d = 4 * grp + (lane & 3);
   const uint32_t ib = (uint32_t)ib064 + d;
   const bool valid = ib < lenb32;
   const int KP = A.KP, noct = KP / 8;
-  const int oct[2] = {lane >> 2, (lane >> 2) + 8};
-  uint64_t mre[2][8], mim[2][8];
-  uint32_t nre[2] = {0u, 0u}, nim[2] = {0u, 0u};
+  const int o = 8 * half + (lane >> 2);
+  const bool live = o < noct && valid;
+  uint64_t mre[8], mim[8];
+  uint32_t nre = 0u, nim = 0u;
   int blr = 0, bli = 0;
 #pragma unroll
-  for (int oi = 0; oi < 2; ++oi)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      long long re, im;
-      gather_d(A, 8 * oct[oi] + j, oct[oi] < noct && valid, ia, ib, lena32, lenb32, re, im);
-      nre[oi] |= (re < 0 ? 1u : 0u) << j;
-      nim[oi] |= (im < 0 ? 1u : 0u) << j;
-      mre[oi][j] = (uint64_t)(re < 0 ? -re : re);
-      mim[oi][j] = (uint64_t)(im < 0 ? -im : im);
-      blr = max(blr, 64 - __clzll((long long)mre[oi][j]));
-      bli = max(bli, 64 - __clzll((long long)mim[oi][j]));
-    }
+  for (int j = 0; j < 8; ++j) {
+    long long re, im;
+    gather_d(A, 8 * o + j, live, ia, ib, lena32, lenb32, re, im);
+    nre |= (re < 0 ? 1u : 0u) << j;
+    nim |= (im < 0 ? 1u : 0u) << j;
+    mre[j] = (uint64_t)(re < 0 ? -re : re);
+    mim[j] = (uint64_t)(im < 0 ? -im : im);
+    blr = max(blr, 64 - __clzll((long long)mre[j]));
+    bli = max(bli, 64 - __clzll((long long)mim[j]));
+  }
 #pragma unroll
   for (int m = 4; m < 32; m <<= 1) {
     blr = max(blr, __shfl_xor_sync(0xffffffffu, blr, m));
     bli = max(bli, __shfl_xor_sync(0xffffffffu, bli, m));
   }
-  if (lane < 4 && valid)
+  if (lane < 4) red[w][lane] = blr | (bli << 8);
+  __syncthreads();
+  const int other = red[w ^ 8][lane & 3];
+  blr = max(blr, other & 0xFF);
+  bli = max(bli, other >> 8);
+  if (half == 0 && lane < 4 && valid)
     A.bexp[ia * lenb32 + ib] = make_uchar2((unsigned char)blr, (unsigned char)bli);
-  uint32_t pk[2][2][2 * kSlices];
+  uint32_t pk[2][2 * kSlices];
 #pragma unroll
-  for (int oi = 0; oi < 2; ++oi) {
+  for (int x = 0; x < 2 * kSlices; ++x) pk[0][x] = pk[1][x] = 0u;
 #pragma unroll
-    for (int x = 0; x < 2 * kSlices; ++x) pk[oi][0][x] = pk[oi][1][x] = 0u;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      pack_slices(pk[oi][0], round40(mre[oi][j], blr - 40), j);
-      pack_slices(pk[oi][1], round40(mim[oi][j], bli - 40), j);
-    }
+  for (int j = 0; j < 8; ++j) {
+    pack_slices(pk[0], round40(mre[j], blr - 40), j);
+    pack_slices(pk[1], round40(mim[j], bli - 40), j);
   }
+  if (o >= noct) return;
   const size_t chunk = (size_t)kN * KP;
   __nv_bfloat16* out = A.dslices + (size_t)t * kSlices * chunk;
 #pragma unroll
@@ -261,19 +267,15 @@ __global__ void __launch_bounds__(kSliceThreads) k_oz_slice(OzArgs A) {
     const uint32_t ebits = (uint32_t)(150 - 8 * b) << 23;
     __nv_bfloat16* dst = out + (size_t)(b - 1) * chunk;
 #pragma unroll
-    for (int oi = 0; oi < 2; ++oi) {
-      if (oct[oi] >= noct) continue;
-#pragma unroll
-      for (int part = 0; part < 2; ++part) {
-        const uint32_t nb = part ? nim[oi] : nre[oi];
-        const uint32_t lo = pk[oi][part][2 * (b - 1)], hi = pk[oi][part][2 * (b - 1) + 1];
-        uint4 v;
-        v.x = bf16_bytes_pair(lo, 0, nb, ebits);
-        v.y = bf16_bytes_pair(lo, 2, nb >> 2, ebits);
-        v.z = bf16_bytes_pair(hi, 0, nb >> 4, ebits);
-        v.w = bf16_bytes_pair(hi, 2, nb >> 6, ebits);
-        *reinterpret_cast<uint4*>(dst + tc::kmajor_offset(2 * d + part, 8 * oct[oi], KP)) = v;
-      }
+    for (int part = 0; part < 2; ++part) {
+      const uint32_t nb = part ? nim : nre;
+      const uint32_t lo = pk[part][2 * (b - 1)], hi = pk[part][2 * (b - 1) + 1];
+      uint4 v;
+      v.x = bf16_bytes_pair(lo, 0, nb, ebits);
+      v.y = bf16_bytes_pair(lo, 2, nb >> 2, ebits);
+      v.z = bf16_bytes_pair(hi, 0, nb >> 4, ebits);
+      v.w = bf16_bytes_pair(hi, 2, nb >> 6, ebits);
+      *reinterpret_cast<uint4*>(dst + tc::kmajor_offset(2 * d + part, 8 * o, KP)) = v;
     }
   }
 }
@@ -420,18 +422,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       }
       tc::fence_after_sync();
       const uint32_t base = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(s * kAccCols);
+      // exponents of the tile's 32 determinants: lane l holds determinant l
+      uchar2 be_l = make_uchar2(0, 0);
+      if (ib0 + lane < A.lenb) be_l = A.bexp[ia * A.lenb + ib0 + lane];
+      const int be_pack = (int)be_l.x | ((int)be_l.y << 8);
       for (int c0 = 0; c0 < kN; c0 += 16) {
         float va[16], vb[16], vc[16], vd[16];
         tc::tmem_ld16(base + c0, va);
         tc::tmem_ld16(base + kN + c0, vb);
         tc::tmem_ld16(base + 2 * kN + c0, vc);
         tc::tmem_ld16(base + 3 * kN + c0, vd);
+        int bes[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) bes[k] = __shfl_sync(0xffffffffu, be_pack, c0 / 2 + k);
         if (p >= A.P) continue;
 #pragma unroll
         for (int j = 0; j < 16; j += 2) {
           const int64_t ib = ib0 + (c0 + j) / 2;
           if (ib >= A.lenb) continue;
-          const uchar2 be = A.bexp[ia * A.lenb + ib];
+          const uchar2 be = make_uchar2((unsigned char)(bes[j / 2] & 0xFF),
+                                        (unsigned char)(bes[j / 2] >> 8));
           float out[4];
 #pragma unroll
           for (int part = 0; part < 2; ++part) {
