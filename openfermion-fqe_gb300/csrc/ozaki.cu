@@ -55,10 +55,10 @@ constexpr int kM = 128;        // MMA M (pairs, padded)
 constexpr int kN = 64;         // MMA N (real columns per tile)
 constexpr int kDets = 32;      // determinants per tile
 constexpr int kMaxRing = 8;    // slice-chunk ring depth (fits shared memory)
-constexpr int kEpiWarps = 4;
-constexpr int kMmaWarp = 4;
-constexpr int kLoadWarp = 5;
-constexpr int kThreads = 6 * 32;
+constexpr int kEpiWarps = 8;   // two per TMEM lane quarter, half the columns each
+constexpr int kMmaWarp = 8;
+constexpr int kLoadWarp = 9;
+constexpr int kThreads = 10 * 32;
 constexpr int kSliceThreads = 512;  // one CTA of k_oz_slice = one tile
 constexpr int kAccs = 4;           // levels 2, 3, 4 and 5..7
 constexpr int kAccCols = kAccs * kN;  // one accumulator set (two sets = 512)
@@ -281,9 +281,10 @@ __global__ void __launch_bounds__(kSliceThreads, 2) k_oz_slice(OzArgs A) {
 }
 
 // ---- contraction: bulk-copied slices, tcgen05 MMAs, TMEM epilogue -----------
-// Persistent, one CTA per SM, 6 warps: warps 0-3 epilogue, warp 4 TMEM
-// allocation + MMA issue (lane 0), warp 5 lane 0 streams the slice images of
-// each tile into a ring of shared-memory slots with cp.async.bulk.
+// Persistent, one CTA per SM, 10 warps: warps 0-7 epilogue (warp w reads TMEM
+// lanes 32 (w % 4) .. + 31, columns of determinants 16 (w / 4) .. + 15), warp 8
+// TMEM allocation + MMA issue (lane 0), warp 9 lane 0 streams the slice images
+// of each tile into a ring of shared-memory slots with cp.async.bulk.
 __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int KP = A.KP, R = A.ring;
@@ -406,7 +407,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       if (!oz_wait(done, 0, abort_flag) && !*abort_flag) oz_abort(abort_flag, A.err, 6);
     }
   } else {
-    const int p = tid;  // TMEM lane = pair row
+    const int quarter = warp & 3, half = warp >> 2;
+    const int p = 32 * quarter + lane;  // TMEM lane = pair row
     const int ev = (p < A.P) ? A.vexp[p] : 0;
     const int g0 = A.misc[0];
     int64_t it = 0;
@@ -414,6 +416,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       int64_t ia, ib0;
       tile_coords(A, t, ia, ib0);
       const int s = (int)(it & 1);
+      // exponents of the tile's 32 determinants: lane l holds determinant l
+      uchar2 be_l = make_uchar2(0, 0);
+      if (ib0 + lane < A.lenb) be_l = A.bexp[ia * A.lenb + ib0 + lane];
+      const int be_pack = (int)be_l.x | ((int)be_l.y << 8);
       const bool got = __all_sync(0xffffffffu,
                                   oz_wait(&accfull[s], (uint32_t)((it >> 1) & 1), abort_flag));
       if (!got) {
@@ -421,39 +427,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
         break;
       }
       tc::fence_after_sync();
-      const uint32_t base = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(s * kAccCols);
-      // exponents of the tile's 32 determinants: lane l holds determinant l
-      uchar2 be_l = make_uchar2(0, 0);
-      if (ib0 + lane < A.lenb) be_l = A.bexp[ia * A.lenb + ib0 + lane];
-      const int be_pack = (int)be_l.x | ((int)be_l.y << 8);
-      for (int c0 = 0; c0 < kN; c0 += 16) {
-        float va[16], vb[16], vc[16], vd[16];
-        tc::tmem_ld16(base + c0, va);
-        tc::tmem_ld16(base + kN + c0, vb);
-        tc::tmem_ld16(base + 2 * kN + c0, vc);
-        tc::tmem_ld16(base + 3 * kN + c0, vd);
+      const uint32_t base =
+          tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(s * kAccCols);
+      float4* grow = A.G + ((int64_t)p * A.lena + ia) * A.lenb + ib0;
+      for (int c0 = 32 * half; c0 < 32 * half + 32; c0 += 16) {
+        uint32_t ra[16], rb[16], rc[16], rd[16];
+        tc::tmem_ld16_nowait(base + c0, ra);
+        tc::tmem_ld16_nowait(base + kN + c0, rb);
+        tc::tmem_ld16_nowait(base + 2 * kN + c0, rc);
+        tc::tmem_ld16_nowait(base + 3 * kN + c0, rd);
+        tc::tmem_wait_ld();
         int bes[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) bes[k] = __shfl_sync(0xffffffffu, be_pack, c0 / 2 + k);
         if (p >= A.P) continue;
 #pragma unroll
         for (int j = 0; j < 16; j += 2) {
-          const int64_t ib = ib0 + (c0 + j) / 2;
-          if (ib >= A.lenb) continue;
-          const uchar2 be = make_uchar2((unsigned char)(bes[j / 2] & 0xFF),
-                                        (unsigned char)(bes[j / 2] >> 8));
+          const int dj = (c0 + j) / 2;
+          if (ib0 + dj >= A.lenb) continue;
           float out[4];
 #pragma unroll
           for (int part = 0; part < 2; ++part) {
             // column exponent: |D| < 2^(bits - 62 + g0)
-            const int sc = ev + (int)(part ? be.y : be.x) - 62 + g0;
-            const float x = va[j + part], y = vb[j + part];
+            const int bits = part ? (bes[j / 2] >> 8) : (bes[j / 2] & 0xFF);
+            const int sc = ev + bits - 62 + g0;
+            const float x = __uint_as_float(ra[j + part]), y = __uint_as_float(rb[j + part]);
             // exact two-sum of levels 2 and 3, then levels 4 and 5..7
             const float h = x + y;
             const float bb = h - x;
             float l = (x - (h - bb)) + (y - bb);
-            l += vc[j + part];
-            l += vd[j + part];
+            l += __uint_as_float(rc[j + part]);
+            l += __uint_as_float(rd[j + part]);
             const float h2 = h + l;
             const float l2 = l - (h2 - h);
             if (sc >= -126 && sc <= 127) {
@@ -465,8 +469,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
               out[2 * part + 1] = scale2(l2, sc);
             }
           }
-          A.G[((int64_t)p * A.lena + ia) * A.lenb + ib] =
-              make_float4(out[0], out[1], out[2], out[3]);
+          grow[dj] = make_float4(out[0], out[1], out[2], out[3]);
         }
       }
       tc::fence_before_sync();
