@@ -198,6 +198,14 @@ int fqegpu_taylor(fqegpu_ham h, double *d_psi, double time, double e0_re,
  * determinant, algorithm/davidson.py:159-180). */
 int fqegpu_diagonal(fqegpu_ham h, double *d_diag, void *stream);
 
+/* Davidson correction vector, complex128[n] -> complex128[n]:
+ *   d_t[I] = d_r[I] / (theta - d_diag[I]),  |theta - d_diag[I]| >= floor_
+ * (the reference's diagonal preconditioner, algorithm/davidson.py:273-280,
+ * where the denominator is computed on the host from the O(N) diagonal). */
+int fqegpu_precondition(int64_t n, const double *d_r, const double *d_diag,
+                        double theta, double floor_, double *d_t,
+                        void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,261 @@
+"""Block Davidson for the lowest eigenpairs of a restricted Hamiltonian on one
+sector (A12 of the path).
+
+The reference (algorithm/davidson.py:140-359) builds its preconditioner
+diagonal with one expectation value per determinant (O(N) applies, :159-180),
+rebuilds the projected matrix from scratch each iteration and stops on the
+change of the eigenvalues (:233).  This driver keeps its entry point and
+return values (`davidson_diagonalization(hamiltonian, n_alpha, n_beta,
+nroots, guess_vecs)` -> (eigenvalues, eigen-wavefunctions)) and is a
+residual-based block Davidson: the diagonal comes from one Slater-Condon pass
+(fqegpu_diagonal), H·v from fqegpu_apply (FP64 or tensor-core), inner products
+and axpys from libfqegpu (FP64, deterministic), the projected eigenproblem
+(<= max_subspace) is solved in FP64 on the host, and a root is converged when
+||H x - theta x|| < tol.  The preconditioned residual is
+t = m * r / (theta - H_II): m = 1 for the diagonal preconditioner, or the
+output of a learned per-determinant correction (fqe_gb300.precond), which can
+change the number of iterations but never the converged energy — the residual
+decides.
+"""
+
+import ctypes
+import time
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy
+import torch
+
+from . import _lib
+from . import settings
+from .fci_graph import get_graph
+from .fqe_data import FqeData, ham_for, _ptr, _stream
+from .hamiltonians import RestrictedHamiltonian
+from .wavefunction import Wavefunction
+
+
+class DiagonalPreconditioner:
+    """t = r / (theta - H_II), |theta - H_II| floored (davidson.py:273-280)."""
+
+    name = "diagonal"
+
+    def __init__(self, floor: float = 1.0e-4):
+        self.floor = floor
+
+    def __call__(self, r: torch.Tensor, theta: float, diag: torch.Tensor,
+                 graph) -> torch.Tensor:
+        t = torch.empty_like(r)
+        _lib.call("fqegpu_precondition", r.numel(), _ptr(r), _ptr(diag),
+                  float(theta), float(self.floor), _ptr(t), _stream())
+        return t
+
+
+@dataclass
+class DavidsonResult:
+    eigenvalues: numpy.ndarray
+    vectors: List[torch.Tensor]
+    iterations: int
+    applies: int
+    converged: bool
+    residual_history: List[List[float]] = field(default_factory=list)
+    seconds: float = 0.0
+
+
+def _vdot(x: torch.Tensor, y: torch.Tensor) -> complex:
+    out = (ctypes.c_double * 2)()
+    _lib.call("fqegpu_vdot", x.numel(), _ptr(x), _ptr(y), out, _stream())
+    return complex(out[0], out[1])
+
+
+def _axpy(a: complex, x: torch.Tensor, y: torch.Tensor) -> None:
+    a = complex(a)
+    _lib.call("fqegpu_axpy", x.numel(), a.real, a.imag, _ptr(x), _ptr(y),
+              _stream())
+
+
+def _norm(x: torch.Tensor) -> float:
+    out = ctypes.c_double()
+    _lib.call("fqegpu_norm2", x.numel(), _ptr(x), ctypes.byref(out), _stream())
+    return out.value
+
+
+def _scale(a: complex, x: torch.Tensor) -> None:
+    a = complex(a)
+    _lib.call("fqegpu_scale", x.numel(), a.real, a.imag, _ptr(x), _stream())
+
+
+class _Operator:
+    """H on one sector: apply, diagonal (both include e_0)."""
+
+    def __init__(self, hamiltonian: RestrictedHamiltonian, nalpha: int,
+                 nbeta: int, precision: Optional[str] = None):
+        tensors = hamiltonian.tensors()
+        self.norb = hamiltonian.dim()
+        self.graph = get_graph(nalpha, nbeta, self.norb)
+        self.e0 = complex(hamiltonian.e_0())
+        self.ham = ham_for(self.graph, tensors[0],
+                           tensors[1] if len(tensors) > 1 else None)
+        self.shape = (self.graph.lena(), self.graph.lenb())
+        self.precision = precision
+        self.applies = 0
+        diag = torch.empty(self.shape, dtype=torch.float64,
+                           device=settings.device())
+        _lib.call("fqegpu_diagonal", self.ham.handle, _ptr(diag), _stream())
+        self.diag = diag + self.e0.real
+
+    def apply(self, v: torch.Tensor) -> torch.Tensor:
+        out = torch.empty_like(v)
+        code = settings.precision_code() if self.precision is None else {
+            "fp64": _lib.PREC_FP64, "ozaki": _lib.PREC_OZAKI}[self.precision]
+        _lib.call("fqegpu_apply", self.ham.handle, _ptr(v), _ptr(out), 1.0,
+                  0.0, self.e0.real, self.e0.imag, code, _stream())
+        self.applies += 1
+        return out
+
+
+def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
+             nroots: int = 1, block: Optional[int] = None, tol: float = 1.0e-6,
+             max_subspace: int = 32, max_iter: int = 200,
+             guess: Optional[List[torch.Tensor]] = None,
+             preconditioner=None, precision: Optional[str] = None,
+             verbose: bool = False) -> DavidsonResult:
+    """Lowest `nroots` eigenpairs of the sector (nalpha, nbeta)."""
+    t_start = time.time()
+    op = _Operator(hamiltonian, nalpha, nbeta, precision)
+    block = max(nroots, block or nroots)
+    if max_subspace < 2 * block:
+        raise ValueError("max_subspace must hold at least two blocks")
+    prec = preconditioner or DiagonalPreconditioner()
+    n = op.shape[0] * op.shape[1]
+    if nroots > n:
+        raise ValueError("Number of roots is incorrectly specified")
+    V: List[torch.Tensor] = []
+    AV: List[torch.Tensor] = []
+
+    def orthonormal_add(t: torch.Tensor) -> bool:
+        for _ in range(2):  # classical Gram-Schmidt, twice
+            for v in V:
+                _axpy(-_vdot(v, t), v, t)
+        nrm = _norm(t)
+        if nrm < 1.0e-10:
+            return False
+        _scale(1.0 / nrm, t)
+        V.append(t)
+        AV.append(op.apply(t))
+        return True
+
+    # initial block: the lowest diagonal determinants (or the caller's guess)
+    if guess:
+        for g in guess:
+            orthonormal_add(g.clone().to(torch.complex128).reshape(op.shape))
+    order = torch.argsort(op.diag.reshape(-1)).cpu().numpy()
+    k = 0
+    while len(V) < block and k < n:
+        e = torch.zeros(op.shape, dtype=torch.complex128, device=op.diag.device)
+        e.view(-1)[int(order[k])] = 1.0
+        orthonormal_add(e)
+        k += 1
+
+    history: List[List[float]] = []
+    T = numpy.zeros((0, 0), dtype=numpy.complex128)
+    converged = False
+    theta = numpy.zeros(nroots)
+    X: List[torch.Tensor] = []
+    it = 0
+    for it in range(1, max_iter + 1):
+        m = len(V)
+        Tn = numpy.zeros((m, m), dtype=numpy.complex128)
+        Tn[:T.shape[0], :T.shape[1]] = T
+        for i in range(m):
+            for j in range(m):
+                if i < T.shape[0] and j < T.shape[1]:
+                    continue
+                Tn[i, j] = _vdot(V[i], AV[j])
+        T = 0.5 * (Tn + Tn.conj().T)
+        w, y = numpy.linalg.eigh(T)
+        X, AX, R, res = [], [], [], []
+        for j in range(block):
+            x = torch.zeros_like(V[0])
+            ax = torch.zeros_like(V[0])
+            for i in range(m):
+                _axpy(y[i, j], V[i], x)
+                _axpy(y[i, j], AV[i], ax)
+            r = ax.clone()
+            _axpy(-w[j], x, r)
+            X.append(x)
+            AX.append(ax)
+            R.append(r)
+            res.append(_norm(r))
+        history.append(res[:nroots])
+        theta = w[:nroots]
+        if verbose:
+            print(f"davidson iter {it}: theta {w[:nroots]} residual {res[:nroots]}")
+        if all(rr < tol for rr in res[:nroots]):
+            converged = True
+            break
+        if m + block > max_subspace:
+            # restart on the current Ritz vectors (orthonormal) and their images
+            V, AV = list(X), list(AX)
+            T = numpy.diag(w[:block]).astype(numpy.complex128)
+        added = 0
+        for j in range(block):
+            if res[j] < tol and j < nroots:
+                continue
+            t = prec(R[j], float(w[j]), op.diag, op.graph)
+            if orthonormal_add(t):
+                added += 1
+        if added == 0:
+            break
+    torch.cuda.synchronize()
+    return DavidsonResult(eigenvalues=numpy.array(theta), vectors=X[:nroots],
+                          iterations=it, applies=op.applies,
+                          converged=converged, residual_history=history,
+                          seconds=time.time() - t_start)
+
+
+def davidsonliu_fqe(hmat: RestrictedHamiltonian, nroots: int, guess_vecs,
+                    nele: int, sz: int, norb: int, epsilon: float = 1.0e-8,
+                    verbose: bool = False, **kwargs):
+    """Reference entry point (algorithm/davidson.py:140-307).  `epsilon` was
+    the eigenvalue-change threshold; here the residual tolerance is
+    100 * epsilon (the eigenvalue error is of the order of the squared
+    residual over the gap).  Same errors: ValueError for a bad root count,
+    TypeError when the guesses lie in different sectors."""
+    if nroots < 1 or nroots > 2**(hmat.dim() - 1):
+        raise ValueError("Number of roots is incorrectly specified")
+    sector = list(guess_vecs[0].sectors())[0]
+    for gv in guess_vecs:
+        if list(gv.sectors())[0] != sector:
+            raise TypeError("Sectors don't match for guess vectors")
+    if sector != (nele, sz) or hmat.dim() != norb:
+        raise ValueError("guess vectors do not match (nele, sz, norb)")
+    nalpha, nbeta = (nele + sz) // 2, (nele - sz) // 2
+    res = davidson(hmat, nalpha, nbeta, nroots=nroots,
+                   guess=[g.get_coeff(sector) for g in guess_vecs],
+                   tol=kwargs.pop("tol", 100.0 * epsilon), verbose=verbose,
+                   **kwargs)
+    return res.eigenvalues, _as_wavefunctions(res.vectors, nele, sz, norb)
+
+
+def _as_wavefunctions(vectors, nele, sz, norb):
+    wfns = []
+    for x in vectors:
+        w = Wavefunction([[nele, sz, norb]])
+        w.set_wfn(strategy="from_data", raw_data={(nele, sz): x})
+        wfns.append(w)
+    return wfns
+
+
+def davidson_diagonalization(hamiltonian: RestrictedHamiltonian, n_alpha: int,
+                             n_beta: int, nroots: int = 1, guess_vecs=None,
+                             **kwargs):
+    """Reference entry point (algorithm/davidson.py:310-359): returns
+    (eigenvalues, list of eigen-Wavefunctions)."""
+    norb = hamiltonian.dim()
+    nele, sz = n_alpha + n_beta, n_alpha - n_beta
+    guess = None
+    if guess_vecs:
+        guess = [g.get_coeff((nele, sz)) for g in guess_vecs]
+    res = davidson(hamiltonian, n_alpha, n_beta, nroots=nroots, guess=guess,
+                   **kwargs)
+    return res.eigenvalues, _as_wavefunctions(res.vectors, nele, sz, norb)

@@ -177,9 +177,48 @@ def dvec_fixture():
     save("dvec", **out)
 
 
+def davidson_fixture():
+    """LiH (norb 6, 2+2 electrons) from the reference's own test data
+    (tests/unittest_data/build_lih_data.py) with the reference Davidson's
+    answer, and the norb-4 Hamiltonian h2[i,j,k,l] = 0.02 (i+k)(j+l) of
+    fqe_data_test.py:763-771 with the reference Davidson's two lowest roots
+    (its eigenvalue-change stopping rule leaves them ~4e-5 above the exact,
+    four-fold degenerate -7.271991091302982 that the same test asserts)."""
+    numpy.infty = numpy.inf  # removed in numpy 2; davidson.py:182 uses it
+    sys.path.insert(0, os.path.join(ref_fqe.REF_ROOT, "tests"))
+    from unittest_data.build_lih_data import build_lih_data
+    from fqe.hamiltonians.restricted_hamiltonian import RestrictedHamiltonian
+    from fqe.algorithm import davidson
+    h1, h2, ground = build_lih_data("energy")
+    ham = RestrictedHamiltonian((h1, h2))
+    numpy.random.seed(3)
+    w_lih, _ = davidson.davidson_diagonalization(ham, 2, 2, nroots=1)
+    wfn = fqe.Wavefunction([[4, 0, 6]])
+    wfn.set_wfn(strategy="from_data", raw_data={(4, 0): ground})
+    e_lih = wfn.expectationValue(ham)
+    norb = 4
+    h2k = numpy.zeros((norb,) * 4, dtype=numpy.complex128)
+    for i in range(norb):
+        for j in range(norb):
+            for k in range(norb):
+                for l in range(norb):
+                    h2k[i, j, k, l] += (i + k) * (j + l) * 0.02
+    h1k = numpy.zeros((norb, norb), dtype=numpy.complex128)
+    numpy.random.seed(4)
+    w_k, _ = davidson.davidson_diagonalization(
+        RestrictedHamiltonian((h1k, h2k)), 2, 2, nroots=2)
+    save("davidson", lih_h1=numpy.asarray(h1), lih_h2=numpy.asarray(h2),
+         lih_ground=numpy.asarray(ground),
+         lih_e_test=numpy.array(-8.877719570384043),
+         lih_e_expectation=numpy.array(e_lih),
+         lih_e_ref_davidson=numpy.asarray(w_lih),
+         k4_h1=h1k, k4_h2=h2k,
+         k4_e_test=numpy.array(-7.271991091302982),
+         k4_e_ref_davidson=numpy.asarray(w_k))
+
+
 if __name__ == "__main__":
-    graph_fixture()
-    apply_fixture()
-    dc_fixture()
-    taylor_fixture()
-    dvec_fixture()
+    which = sys.argv[1:] or ["graph", "apply", "dc", "taylor", "dvec",
+                             "davidson"]
+    for name in which:
+        globals()[name + "_fixture"]()

@@ -192,3 +192,25 @@ def test_live_reference_random_cases(oracle):
         assert _rel(oracle.apply_spatial12(c, h1, h2, g), ref) < 1e-13
         numpy.testing.assert_array_equal(g.dexca, d._core._dexca)
         numpy.testing.assert_array_equal(g.astr, d._core._astr)
+
+
+def test_davidson_known_answers_dense(golden, oracle):
+    # The oracle's dense H (unit-vector applies) reproduces the two energies
+    # the reference's tests assert: LiH ground state -8.877719570384043
+    # (tests/davidson_test.py:27, with build_lih_data's integrals) and the
+    # four-fold degenerate -7.271991091302982 of fqe_data_test.py:766.
+    gd = golden("davidson")
+    g = oracle.graph(6, 2, 2)
+    H = oracle.dense_hamiltonian(gd["lih_h1"].astype(complex),
+                                 gd["lih_h2"].astype(complex), g)
+    w = numpy.linalg.eigvalsh(0.5 * (H + H.conj().T))
+    assert abs(w[0] - float(gd["lih_e_test"])) < 1e-10
+    psi = gd["lih_ground"].ravel()
+    assert abs(numpy.vdot(psi, H @ psi) - gd["lih_e_expectation"]) < 1e-12
+    assert abs(float(gd["lih_e_ref_davidson"][0]) - w[0]) < 1e-8
+    g4 = oracle.graph(4, 2, 2)
+    H4 = oracle.dense_hamiltonian(gd["k4_h1"], gd["k4_h2"], g4)
+    w4 = numpy.linalg.eigvalsh(0.5 * (H4 + H4.conj().T))
+    assert numpy.allclose(w4[:4], float(gd["k4_e_test"]), atol=1e-12)
+    # the reference Davidson's eigenvalue-change rule stops above the exact root
+    assert 1e-6 < gd["k4_e_ref_davidson"][0] - w4[0] < 1e-3
