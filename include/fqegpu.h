@@ -206,6 +206,49 @@ int fqegpu_precondition(int64_t n, const double *d_r, const double *d_diag,
                         double theta, double floor_, double *d_t,
                         void *stream);
 
+/* ---- A12: learned Davidson preconditioner ---------------------------------
+ * No counterpart in the reference (its Davidson uses the plain diagonal
+ * preconditioner, algorithm/davidson.py:273-280).  A 34 -> 64 -> 64 -> 1 MLP
+ * (bfloat16 weights, float32 sums) gives each determinant a multiplier
+ * m_I in (0, 2) of the diagonal preconditioner:
+ *   d_t[I] = m_I d_r[I] / (theta - d_diag[I])   (|denominator| >= floor_)
+ * Features: (H_II - theta) / scale, (theta - emin) / scale and the alpha and
+ * beta occupations of 16 slots each, slot k holding orbital k - 8 + n_spin
+ * (core slots read 1).  norb <= 16.  Parameters (float32, in this order):
+ * W1[64][34], b1[64], W2[64][64], b2[64], w3[64], b3 — 6465 values.  A new
+ * network has all parameters zero (m = 1: the plain preconditioner). */
+typedef struct fqegpu_mlp_s *fqegpu_mlp;
+int fqegpu_mlp_create(fqegpu_mlp *out);
+int fqegpu_mlp_destroy(fqegpu_mlp m);
+int fqegpu_mlp_nparams(void);
+/* Sets the float32 master copy (and its bfloat16 image); resets Adam. */
+int fqegpu_mlp_set_params(fqegpu_mlp m, const float *h_params, int64_t n);
+int fqegpu_mlp_get_params(fqegpu_mlp m, float *h_params, int64_t n);
+int fqegpu_mlp_get_grad(fqegpu_mlp m, float *h_grad, int64_t n);
+/* Inference fused with preconditioning (complex128 r, t; float64 diag). */
+int fqegpu_mlp_precondition(fqegpu_mlp m, fqegpu_graph g, const double *d_r,
+                            const double *d_diag, double theta, double scale,
+                            double emin, double floor_, double *d_t,
+                            void *stream);
+/* The multipliers alone (float32 [lena * lenb]). */
+int fqegpu_mlp_multiplier(fqegpu_mlp m, fqegpu_graph g, const double *d_diag,
+                          double theta, double scale, double emin, float *d_m,
+                          void *stream);
+/* One correction-equation sample: u = r / (theta - H_II) (floored), Ritz
+ * vector x, exact correction a (a orthogonal to x), all complex128.  Loss
+ *   L = 1 - |a^H v|^2 / (|a|^2 |v|^2),  v = (1 - x x^H)(m * u)
+ * to *h_loss; d L / d params stored in the handle (added to the stored
+ * gradient when accumulate != 0).  Synchronises on `stream`. */
+int fqegpu_mlp_loss_grad(fqegpu_mlp m, fqegpu_graph g, const double *d_u,
+                         const double *d_x, const double *d_a,
+                         const double *d_diag, double theta, double scale,
+                         double emin, int accumulate, double *h_loss,
+                         void *stream);
+/* Adam on the master copy with gradient * grad_scale; refreshes the bfloat16
+ * weights. */
+int fqegpu_mlp_adam(fqegpu_mlp m, double lr, double beta1, double beta2,
+                    double eps, double grad_scale, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -61,6 +61,16 @@ _SIGNATURES = {
                       ctypes.POINTER(_I), _P],
     "fqegpu_diagonal": [_P, _P, _P],
     "fqegpu_precondition": [_L, _P, _P, _D, _D, _P, _P],
+    "fqegpu_mlp_create": [ctypes.POINTER(_P)],
+    "fqegpu_mlp_destroy": [_P],
+    "fqegpu_mlp_nparams": [],
+    "fqegpu_mlp_set_params": [_P, _P, _L],
+    "fqegpu_mlp_get_params": [_P, _P, _L],
+    "fqegpu_mlp_get_grad": [_P, _P, _L],
+    "fqegpu_mlp_precondition": [_P, _P, _P, _P, _D, _D, _D, _D, _P, _P],
+    "fqegpu_mlp_multiplier": [_P, _P, _P, _D, _D, _D, _P, _P],
+    "fqegpu_mlp_loss_grad": [_P, _P, _P, _P, _P, _P, _D, _D, _D, _I, _P, _P],
+    "fqegpu_mlp_adam": [_P, _D, _D, _D, _D, _D, _P],
 }
 
 _lib = None

@@ -104,11 +104,15 @@ class _Operator:
         self.diag = diag + self.e0.real
 
     def apply(self, v: torch.Tensor) -> torch.Tensor:
+        return self.apply_shifted(v, 0.0)
+
+    def apply_shifted(self, v: torch.Tensor, shift: float) -> torch.Tensor:
+        """(H + shift) v."""
         out = torch.empty_like(v)
         code = settings.precision_code() if self.precision is None else {
             "fp64": _lib.PREC_FP64, "ozaki": _lib.PREC_OZAKI}[self.precision]
         _lib.call("fqegpu_apply", self.ham.handle, _ptr(v), _ptr(out), 1.0,
-                  0.0, self.e0.real, self.e0.imag, code, _stream())
+                  0.0, self.e0.real + shift, self.e0.imag, code, _stream())
         self.applies += 1
         return out
 
@@ -118,8 +122,12 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
              max_subspace: int = 32, max_iter: int = 200,
              guess: Optional[List[torch.Tensor]] = None,
              preconditioner=None, precision: Optional[str] = None,
-             verbose: bool = False) -> DavidsonResult:
-    """Lowest `nroots` eigenpairs of the sector (nalpha, nbeta)."""
+             verbose: bool = False, callback=None) -> DavidsonResult:
+    """Lowest `nroots` eigenpairs of the sector (nalpha, nbeta).
+
+    `callback(iteration, ritz_vectors, residuals, ritz_values, operator)` is
+    called once per iteration before the subspace is expanded (the learned
+    preconditioner's training samples are taken there)."""
     t_start = time.time()
     op = _Operator(hamiltonian, nalpha, nbeta, precision)
     block = max(nroots, block or nroots)
@@ -188,6 +196,8 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
             res.append(_norm(r))
         history.append(res[:nroots])
         theta = w[:nroots]
+        if callback is not None and not all(rr < tol for rr in res[:nroots]):
+            callback(it, X, R, w, op)
         if verbose:
             print(f"davidson iter {it}: theta {w[:nroots]} residual {res[:nroots]}")
         if all(rr < tol for rr in res[:nroots]):
@@ -204,6 +214,11 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
             t = prec(R[j], float(w[j]), op.diag, op.graph)
             if orthonormal_add(t):
                 added += 1
+            elif hasattr(prec, "plain"):
+                # the learned vector lies in the subspace: plain fallback
+                if orthonormal_add(prec.plain(R[j], float(w[j]), op.diag,
+                                              op.graph)):
+                    added += 1
         if added == 0:
             break
     torch.cuda.synchronize()
