@@ -12,6 +12,10 @@ both larger than the 129 MB L2); `e2e` times the same apply through the C ABI
 entry fqegpu_apply_host with pinned host buffers (host->device copy of psi and
 device->host copy of sigma inside the timed region).  Under torchrun every
 rank runs an independent replica (the path does not shard); rank 0 prints.
+
+The second half of the metric, Davidson time to a 1e-6 residual with the
+learned vs the plain diagonal preconditioner, is the "davidson" object of the
+same line (default sector norb=12 (6a,6b); --davidson-norb, --no-davidson).
 """
 
 import argparse
@@ -30,7 +34,8 @@ sys.path.insert(0, os.path.join(REPO, "openfermion-fqe_gb300"))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 NORB, NALPHA, NBETA, NCHOL, SEED = 14, 7, 7, 28, 0
-METRIC = "H*psi det-updates/s at norb=14"
+METRIC = ("H*psi det-updates/s at norb=14; Davidson time-to-1e-6 resid, "
+          "learned vs plain")
 
 
 def set_workload(norb, nalpha, nbeta, nchol):
@@ -357,11 +362,52 @@ def run_gpu(args):
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
+    if rank == 0 and world == 1 and not args.no_davidson:
+        line["davidson"] = davidson_leg(args.davidson_norb)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def davidson_leg(norb):
+    """Davidson to a 1e-6 residual on one sector, plain diagonal vs learned
+    preconditioner, same GPU, same seeded synthetic integrals."""
+    import torch
+    import fqe_gb300
+    from fqe_gb300 import davidson as dav, precond, synthetic
+    na, nb = norb // 2, norb - norb // 2
+    nchol = synthetic.default_nchol(norb)
+    h1, h2, _ = synthetic.integrals(norb, nchol, SEED)
+    ham = fqe_gb300.RestrictedHamiltonian((h1, h2))
+    kw = dict(block=4, tol=1e-6, max_subspace=32, max_iter=400)
+    dav.davidson(ham, na, nb, **dict(kw, max_iter=2))  # plans, tables, caches
+    torch.cuda.synchronize()
+
+    def row(r, extra=None):
+        d = {"seconds": r.seconds, "iterations": r.iterations,
+             "applies": r.applies, "energy": float(r.eigenvalues[0]),
+             "converged": bool(r.converged),
+             "final_residual": float(r.residual_history[-1][0])}
+        d.update(extra or {})
+        return d
+
+    plain = dav.davidson(ham, na, nb, **kw)
+    out = {"workload": f"lowest root, norb={norb} ({na}a,{nb}b), {nchol} "
+                       f"Cholesky vectors, seed {SEED}; block 4, subspace <= 32,"
+                       " residual 1e-6",
+           "plain": row(plain), "learned": None}
+    if os.path.exists(precond.DEFAULT_WEIGHTS):
+        pre = precond.LearnedPreconditioner.load()
+        learned = dav.davidson(ham, na, nb, preconditioner=pre, **kw)
+        out["learned"] = row(learned, {"fallbacks": pre.fallbacks})
+        out["energy_difference"] = float(learned.eigenvalues[0]
+                                         - plain.eigenvalues[0])
+        out["time_ratio_learned_over_plain"] = learned.seconds / plain.seconds
+    else:
+        out["note"] = "no trained preconditioner weights in the package"
+    return out
 
 
 def _block_w(ham):
@@ -387,6 +433,9 @@ def main():
     ap.add_argument("--nalpha", type=int, default=None)
     ap.add_argument("--nbeta", type=int, default=None)
     ap.add_argument("--nchol", type=int, default=None)
+    ap.add_argument("--no-davidson", action="store_true",
+                    help="skip the Davidson (plain vs learned) leg")
+    ap.add_argument("--davidson-norb", type=int, default=12)
     args = ap.parse_args()
     if args.norb != 14 or args.nalpha is not None or args.nbeta is not None:
         na = args.nalpha if args.nalpha is not None else args.norb // 2

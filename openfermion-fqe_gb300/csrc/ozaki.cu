@@ -54,7 +54,9 @@ constexpr int kMaxLevel = 7;   // pairs (a, b) with a + b <= 7 are contracted
 constexpr int kM = 128;        // MMA M (pairs, padded)
 constexpr int kN = 64;         // MMA N (real columns per tile)
 constexpr int kDets = 32;      // determinants per tile
-constexpr int kMaxRing = 8;    // slice-chunk ring depth (fits shared memory)
+constexpr int kChunkK = 16;    // K columns per streamed slice chunk (one MMA k-step)
+constexpr int kChunkElems = kN * kChunkK;  // 1024 BF16 = 2 KB
+constexpr int kMaxRing = 64;   // chunk ring depth (bounded by shared memory)
 constexpr int kEpiWarps = 8;   // two per TMEM lane quarter, half the columns each
 constexpr int kMmaWarp = 8;
 constexpr int kLoadWarp = 9;
@@ -260,8 +262,10 @@ __global__ void __launch_bounds__(kSliceThreads, 2) k_oz_slice(OzArgs A) {
     pack_slices(pk[1], round40(mim[j], bli - 40), j);
   }
   if (o >= noct) return;
+  // tile image: [slice][K chunk][64 x 16 canonical K-major], 2 KB per chunk
   const size_t chunk = (size_t)kN * KP;
   __nv_bfloat16* out = A.dslices + (size_t)t * kSlices * chunk;
+  const uint32_t coff = (uint32_t)(o >> 1) * kChunkElems;
 #pragma unroll
   for (int b = 1; b <= kSlices; ++b) {
     const uint32_t ebits = (uint32_t)(150 - 8 * b) << 23;
@@ -275,7 +279,8 @@ __global__ void __launch_bounds__(kSliceThreads, 2) k_oz_slice(OzArgs A) {
       v.y = bf16_bytes_pair(lo, 2, nb >> 2, ebits);
       v.z = bf16_bytes_pair(hi, 0, nb >> 4, ebits);
       v.w = bf16_bytes_pair(hi, 2, nb >> 6, ebits);
-      *reinterpret_cast<uint4*>(dst + tc::kmajor_offset(2 * d + part, 8 * o, KP)) = v;
+      *reinterpret_cast<uint4*>(dst + coff + tc::kmajor_offset(2 * d + part, 8 * (o & 1), kChunkK)) =
+          v;
     }
   }
 }
@@ -289,8 +294,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int KP = A.KP, R = A.ring;
   const uint32_t v_elems = (uint32_t)kM * KP;
-  const uint32_t slot_elems = (uint32_t)kN * KP;
+  const uint32_t slot_elems = (uint32_t)kChunkElems;
   const uint32_t slot_bytes = slot_elems * 2u;
+  const int nch = KP / kChunkK;  // chunks per slice
   __nv_bfloat16* sV = reinterpret_cast<__nv_bfloat16*>(smem);
   __nv_bfloat16* sD = sV + kSlices * v_elems;
   uint64_t* full = reinterpret_cast<uint64_t*>(sD + (size_t)R * slot_elems);
@@ -337,10 +343,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
     if (lane == 0) {
       int64_t it = 0;
       for (int64_t t = t_begin; t < t_end; ++t, ++it) {
-        const __nv_bfloat16* src = A.dslices + (size_t)t * kSlices * slot_elems;
+        const __nv_bfloat16* src = A.dslices + (size_t)t * kSlices * nch * slot_elems;
         bool ok = true;
-        for (int b = 0; b < kSlices; ++b) {
-          const int64_t g = it * kSlices + b;
+        for (int b = 0; b < kSlices * nch; ++b) {
+          const int64_t g = it * kSlices * nch + b;
           const int slot = (int)(g % R);
           if (!oz_wait(&empty[slot], (uint32_t)(((g / R) & 1) ^ 1), abort_flag)) {
             oz_abort(abort_flag, A.err, 5);
@@ -357,8 +363,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   } else if (warp == kMmaWarp) {
     if (lane == 0) {
       const uint32_t idesc = tc::make_idesc_bf16(kM, kN);
-      const uint32_t sbo = (uint32_t)KP * 16u;
-      const int ksteps = KP / 16;
+      const uint32_t sbo = (uint32_t)KP * 16u;          // V: full-K rows
+      const uint32_t sbo_c = (uint32_t)kChunkK * 16u;   // D chunk: 16-column rows
       // descriptors of k-step 0; k-step ks adds 256 bytes = 16 address units
       uint64_t adesc0[kSlices];
       for (int a = 0; a < kSlices; ++a)
@@ -374,30 +380,32 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
         const uint32_t acc0 = tmem + (uint32_t)(s * kAccCols);
         bool first[kAccs] = {true, true, true, true};
         bool ok = true;
+        // chunk (b, c): the 16 K columns c of D slice b; each is released as
+        // soon as its MMAs complete, so the loader runs many chunks ahead
         for (int b = 1; b <= kSlices && ok; ++b) {
-          const int64_t g = it * kSlices + (b - 1);
-          const int slot = (int)(g % R);
-          if (!oz_wait(&full[slot], (uint32_t)((g / R) & 1), abort_flag)) {
-            oz_abort(abort_flag, A.err, 3);
-            ok = false;
-            break;
-          }
-          tc::fence_after_sync();
-          const uint64_t bd0 =
-              tc::make_sdesc(tc::smem_u32(sD + (size_t)slot * slot_elems), 128, sbo);
           const int amax = min(kSlices, kMaxLevel - b);
-          for (int a = 1; a <= amax; ++a) {
-            const int lvl = a + b;
-            const int ai = lvl <= 4 ? lvl - 2 : 3;
-            const uint32_t acc = acc0 + (uint32_t)(ai * kN);
-            const uint64_t ad0 = adesc0[a - 1];
-            for (int ks = 0; ks < ksteps; ++ks) {
-              tc::mma_bf16(acc, ad0 + (uint64_t)(16 * ks), bd0 + (uint64_t)(16 * ks), idesc,
-                           (first[ai] && ks == 0) ? 0u : 1u);
+          for (int c = 0; c < nch; ++c) {
+            const int64_t g = (it * kSlices + (b - 1)) * nch + c;
+            const int slot = (int)(g % R);
+            if (!oz_wait(&full[slot], (uint32_t)((g / R) & 1), abort_flag)) {
+              oz_abort(abort_flag, A.err, 3);
+              ok = false;
+              break;
             }
-            first[ai] = false;
+            tc::fence_after_sync();
+            const uint64_t bd =
+                tc::make_sdesc(tc::smem_u32(sD + (size_t)slot * slot_elems), 128, sbo_c);
+            for (int a = 1; a <= amax; ++a) {
+              const int lvl = a + b;
+              const int ai = lvl <= 4 ? lvl - 2 : 3;
+              const uint32_t acc = acc0 + (uint32_t)(ai * kN);
+              // A (V slice a) advances 256 bytes = 16 descriptor units per k-step
+              tc::mma_bf16(acc, adesc0[a - 1] + (uint64_t)(16 * c), bd, idesc,
+                           first[ai] ? 0u : 1u);
+              first[ai] = false;
+            }
+            tc::mma_commit(&empty[slot]);
           }
-          tc::mma_commit(&empty[slot]);
         }
         if (!ok) break;
         tc::mma_commit(&accfull[s]);
@@ -411,6 +419,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
     const int p = 32 * quarter + lane;  // TMEM lane = pair row
     const int ev = (p < A.P) ? A.vexp[p] : 0;
     const int g0 = A.misc[0];
+    const bool v8 = (A.lenb & 1) == 0;  // G rows start on 32-byte boundaries
     int64_t it = 0;
     for (int64_t t = t_begin; t < t_end; ++t, ++it) {
       int64_t ia, ib0;
@@ -441,11 +450,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) bes[k] = __shfl_sync(0xffffffffu, be_pack, c0 / 2 + k);
         if (p >= A.P) continue;
+        float out[8][4];  // determinants c0/2 .. c0/2 + 7: re hi, re lo, im hi, im lo
 #pragma unroll
         for (int j = 0; j < 16; j += 2) {
-          const int dj = (c0 + j) / 2;
-          if (ib0 + dj >= A.lenb) continue;
-          float out[4];
 #pragma unroll
           for (int part = 0; part < 2; ++part) {
             // column exponent: |D| < 2^(bits - 62 + g0)
@@ -462,14 +469,32 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
             const float l2 = l - (h2 - h);
             if (sc >= -126 && sc <= 127) {
               const float f = pow2f(sc);
-              out[2 * part] = h2 * f;
-              out[2 * part + 1] = l2 * f;
+              out[j / 2][2 * part] = h2 * f;
+              out[j / 2][2 * part + 1] = l2 * f;
             } else {
-              out[2 * part] = scale2(h2, sc);
-              out[2 * part + 1] = scale2(l2, sc);
+              out[j / 2][2 * part] = scale2(h2, sc);
+              out[j / 2][2 * part + 1] = scale2(l2, sc);
             }
           }
-          grow[dj] = make_float4(out[0], out[1], out[2], out[3]);
+        }
+        const int d0 = c0 / 2;
+        if (v8 && ib0 + d0 + 8 <= A.lenb) {
+          // full 32-byte sectors: two determinants per store (row start and
+          // d0 are even, lenb is even, so every address is 32-byte aligned)
+#pragma unroll
+          for (int k = 0; k < 8; k += 2) {
+            float* q = reinterpret_cast<float*>(grow + d0 + k);
+            asm volatile(
+                "st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(q),
+                "f"(out[k][0]), "f"(out[k][1]), "f"(out[k][2]), "f"(out[k][3]),
+                "f"(out[k + 1][0]), "f"(out[k + 1][1]), "f"(out[k + 1][2]), "f"(out[k + 1][3])
+                : "memory");
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            if (ib0 + d0 + k < A.lenb)
+              grow[d0 + k] = make_float4(out[k][0], out[k][1], out[k][2], out[k][3]);
         }
       }
       tc::fence_before_sync();
@@ -649,9 +674,9 @@ static int plan_create(fqegpu_ham h) {
   FQE_CUDA(cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const size_t fixed = sizeof(__nv_bfloat16) * (size_t)kSlices * vel +
                        sizeof(uint64_t) * (2 * kMaxRing + 5) + 16;
-  const size_t slot = sizeof(__nv_bfloat16) * (size_t)kN * KP;
+  const size_t slot = sizeof(__nv_bfloat16) * (size_t)kChunkElems;
   pl->ring = (int)std::min<size_t>(kMaxRing, ((size_t)smax - fixed) / slot);
-  if (pl->ring < 2) {
+  if (pl->ring < 2 * kSlices) {
     set_error("shared memory too small for the tensor-core contraction");
     return FQEGPU_ERR_UNSUPPORTED;
   }

@@ -50,6 +50,18 @@ class DiagonalPreconditioner:
         return t
 
 
+class _PlainOf:
+    """The plain preconditioner of a learned one (after the judge's switch)."""
+
+    name = "diagonal"
+
+    def __init__(self, learned):
+        self.learned = learned
+
+    def __call__(self, r, theta, diag, graph):
+        return self.learned.plain(r, theta, diag, graph)
+
+
 @dataclass
 class DavidsonResult:
     eigenvalues: numpy.ndarray
@@ -59,6 +71,7 @@ class DavidsonResult:
     converged: bool
     residual_history: List[List[float]] = field(default_factory=list)
     seconds: float = 0.0
+    fallback_iteration: Optional[int] = None  # learned -> plain switch
 
 
 def _vdot(x: torch.Tensor, y: torch.Tensor) -> complex:
@@ -122,12 +135,18 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
              max_subspace: int = 32, max_iter: int = 200,
              guess: Optional[List[torch.Tensor]] = None,
              preconditioner=None, precision: Optional[str] = None,
-             verbose: bool = False, callback=None) -> DavidsonResult:
+             verbose: bool = False, callback=None,
+             patience: int = 10) -> DavidsonResult:
     """Lowest `nroots` eigenpairs of the sector (nalpha, nbeta).
 
     `callback(iteration, ritz_vectors, residuals, ritz_values, operator)` is
     called once per iteration before the subspace is expanded (the learned
-    preconditioner's training samples are taken there)."""
+    preconditioner's training samples are taken there).
+
+    A preconditioner with a `plain` method (the learned one) is judged by the
+    residual: when the largest residual of the wanted roots has not halved
+    over `patience` iterations, the rest of the run uses the plain diagonal
+    preconditioner (`fallback_iteration` records when)."""
     t_start = time.time()
     op = _Operator(hamiltonian, nalpha, nbeta, precision)
     block = max(nroots, block or nroots)
@@ -167,6 +186,8 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
     history: List[List[float]] = []
     T = numpy.zeros((0, 0), dtype=numpy.complex128)
     converged = False
+    fallback_it = None
+    best_hist: List[float] = []
     theta = numpy.zeros(nroots)
     X: List[torch.Tensor] = []
     it = 0
@@ -195,6 +216,13 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
             R.append(r)
             res.append(_norm(r))
         history.append(res[:nroots])
+        worst = max(res[:nroots])
+        best_hist.append(min(worst, best_hist[-1]) if best_hist else worst)
+        if (fallback_it is None and hasattr(prec, "plain")
+                and len(best_hist) > patience
+                and best_hist[-1] > 0.5 * best_hist[-1 - patience]):
+            fallback_it = it
+            prec = _PlainOf(prec)
         theta = w[:nroots]
         if callback is not None and not all(rr < tol for rr in res[:nroots]):
             callback(it, X, R, w, op)
@@ -222,7 +250,8 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
         if added == 0:
             break
     torch.cuda.synchronize()
-    return DavidsonResult(eigenvalues=numpy.array(theta), vectors=X[:nroots],
+    return DavidsonResult(fallback_iteration=fallback_it,
+                          eigenvalues=numpy.array(theta), vectors=X[:nroots],
                           iterations=it, applies=op.applies,
                           converged=converged, residual_history=history,
                           seconds=time.time() - t_start)
