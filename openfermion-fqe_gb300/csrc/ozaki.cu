@@ -22,21 +22,25 @@
 // four accumulators are combined into an FP32 pair (hi + lo, ~48 bits) and
 // scaled by 2^{eV(p) + E(I)}.
 //
-// D is never written to HBM: producer warps gather it from a 62-bit
-// fixed-point copy of psi (global scale) through the per-pair target tables,
-// cut it into slices and store them in the canonical no-swizzle K-major
-// layout in shared memory.  One thread issues tcgen05.mma; four epilogue
-// warps drain the accumulators (double-buffered in TMEM) into G, stored as
-// FP32 pairs [P][lena][lenb].  The scatter then runs in FP32-pair arithmetic.
-//
-// Persistent kernel, one CTA per SM, 13 warps:
-//   warps 0-3  epilogue (warp w reads TMEM lanes 32w..32w+31 = pairs p)
-//   warp 4     TMEM allocation; lane 0 issues the MMAs
-//   warps 5-12 producers
-// Tiles are 32 determinants of one alpha row (64 real columns = MMA N),
-// visited in column super-blocks of 1024 so the alpha-source rows stay in L2.
-// Every wait is bounded; on a timeout the kernel records an error, lets the
-// other roles leave, and frees its TMEM.
+// Three kernels:
+//   k_oz_slice  one CTA per tile of 32 determinants (one alpha row): gathers
+//               D from a 62-bit fixed-point copy of psi through the per-pair
+//               target tables, finds each real column's exact exponent, cuts
+//               the values into the five BF16 slices and writes them to HBM
+//               already in the tensor core's shared-memory image (canonical
+//               no-swizzle K-major, 16-column K chunks, the two tiles of a
+//               tile pair interleaved chunk by chunk).
+//   k_oz_mma    persistent, one CTA per SM: a loader lane streams the slice
+//               images with cp.async.bulk into a ring of 16 KB slots (four K
+//               chunks of a tile pair each); one thread issues 128 x 128 x 16
+//               tcgen05.mma (A = V slices resident in shared memory, B = 64
+//               determinants); sixteen epilogue warps combine the four
+//               accumulators (single-buffered, 512 TMEM columns) into G,
+//               stored as FP32 pairs [P][lena][lenb] with 32-byte stores.
+//   k_oz_scatter  sigma from G in FP32-pair arithmetic (k_oz_rowexp,
+//               k_oz_globalexp and k_oz_fixed prepare the fixed-point psi).
+// Every wait in k_oz_mma is bounded; on a timeout the kernel records an
+// error, lets the other roles leave, and frees its TMEM.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -52,19 +56,21 @@ namespace {
 constexpr int kSlices = 5;
 constexpr int kMaxLevel = 7;   // pairs (a, b) with a + b <= 7 are contracted
 constexpr int kM = 128;        // MMA M (pairs, padded)
-constexpr int kN = 64;         // MMA N (real columns per tile)
-constexpr int kDets = 32;      // determinants per tile
+constexpr int kN = 64;         // real columns of one slice tile
+constexpr int kNM = 128;       // MMA N: two slice tiles
+constexpr int kDets = 32;      // determinants per slice tile
 constexpr int kChunkK = 16;    // K columns per streamed slice chunk (one MMA k-step)
 constexpr int kChunkElems = kN * kChunkK;  // 1024 BF16 = 2 KB
+constexpr int kPairChunkElems = 2 * kChunkElems;  // a K chunk of both tiles of a pair: 4 KB
+constexpr int kGroupK = 4;     // chunks per ring slot: one bulk copy, one wait, one commit
 constexpr int kMaxRing = 64;   // chunk ring depth (bounded by shared memory)
-constexpr int kEpiWarps = 8;   // two per TMEM lane quarter, half the columns each
-constexpr int kMmaWarp = 8;
-constexpr int kLoadWarp = 9;
-constexpr int kThreads = 10 * 32;
+constexpr int kEpiWarps = 16;  // four per TMEM lane quarter, 32 columns each
+constexpr int kMmaWarp = 16;
+constexpr int kLoadWarp = 17;
+constexpr int kThreads = 18 * 32;
 constexpr int kSliceThreads = 512;  // one CTA of k_oz_slice = one tile
 constexpr int kAccs = 4;           // levels 2, 3, 4 and 5..7
-constexpr int kAccCols = kAccs * kN;  // one accumulator set (two sets = 512)
-constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kTmemCols = kAccs * kNM;  // 512: one accumulator set
 constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 constexpr int kExpZero = -2000;
 }  // namespace
@@ -110,6 +116,7 @@ __device__ __forceinline__ void tile_coords(const OzArgs& A, int64_t t, int64_t&
 // Bounded wait that also gives up when another role has aborted.
 __device__ __forceinline__ bool oz_wait(uint64_t* bar, uint32_t parity,
                                         volatile int* abort_flag) {
+  if (tc::mbar_try_wait(bar, parity)) return true;  // fast path: no clock read
   const long long t0 = clock64();
   for (uint32_t it = 0;; ++it) {
     if (tc::mbar_try_wait(bar, parity)) return true;
@@ -262,48 +269,63 @@ __global__ void __launch_bounds__(kSliceThreads, 2) k_oz_slice(OzArgs A) {
     pack_slices(pk[1], round40(mim[j], bli - 40), j);
   }
   if (o >= noct) return;
-  // tile image: [slice][K chunk][64 x 16 canonical K-major], 2 KB per chunk
-  const size_t chunk = (size_t)kN * KP;
-  __nv_bfloat16* out = A.dslices + (size_t)t * kSlices * chunk;
-  const uint32_t coff = (uint32_t)(o >> 1) * kChunkElems;
+  // image of a tile pair: [slice][K chunk][tile of the pair][64 x 16 canonical
+  // K-major], so one K chunk of both tiles (4 KB) is the 128-row B operand
+  const size_t chunk = (size_t)(KP / kChunkK) * kPairChunkElems;  // one slice
+  __nv_bfloat16* out = A.dslices + (size_t)(t >> 1) * kSlices * chunk;
+  const uint32_t coff = (uint32_t)(o >> 1) * kPairChunkElems + (uint32_t)(t & 1) * kChunkElems;
 #pragma unroll
   for (int b = 1; b <= kSlices; ++b) {
     const uint32_t ebits = (uint32_t)(150 - 8 * b) << 23;
     __nv_bfloat16* dst = out + (size_t)(b - 1) * chunk;
+    uint32_t v[2][4];
 #pragma unroll
     for (int part = 0; part < 2; ++part) {
       const uint32_t nb = part ? nim : nre;
       const uint32_t lo = pk[part][2 * (b - 1)], hi = pk[part][2 * (b - 1) + 1];
-      uint4 v;
-      v.x = bf16_bytes_pair(lo, 0, nb, ebits);
-      v.y = bf16_bytes_pair(lo, 2, nb >> 2, ebits);
-      v.z = bf16_bytes_pair(hi, 0, nb >> 4, ebits);
-      v.w = bf16_bytes_pair(hi, 2, nb >> 6, ebits);
-      *reinterpret_cast<uint4*>(dst + coff + tc::kmajor_offset(2 * d + part, 8 * (o & 1), kChunkK)) =
-          v;
+      v[part][0] = bf16_bytes_pair(lo, 0, nb, ebits);
+      v[part][1] = bf16_bytes_pair(lo, 2, nb >> 2, ebits);
+      v[part][2] = bf16_bytes_pair(hi, 0, nb >> 4, ebits);
+      v[part][3] = bf16_bytes_pair(hi, 2, nb >> 6, ebits);
     }
+    // rows 2d (real part) and 2d + 1 (imaginary part) are the two adjacent
+    // 16-byte rows of one core matrix: one 32-byte store (2d is even, so the
+    // address is 32-byte aligned)
+    __nv_bfloat16* q = dst + coff + tc::kmajor_offset(2 * d, 8 * (o & 1), kChunkK);
+    asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(q), "r"(v[0][0]),
+                 "r"(v[0][1]), "r"(v[0][2]), "r"(v[0][3]), "r"(v[1][0]), "r"(v[1][1]),
+                 "r"(v[1][2]), "r"(v[1][3])
+                 : "memory");
   }
 }
 
 // ---- contraction: bulk-copied slices, tcgen05 MMAs, TMEM epilogue -----------
-// Persistent, one CTA per SM, 10 warps: warps 0-7 epilogue (warp w reads TMEM
-// lanes 32 (w % 4) .. + 31, columns of determinants 16 (w / 4) .. + 15), warp 8
-// TMEM allocation + MMA issue (lane 0), warp 9 lane 0 streams the slice images
-// of each tile into a ring of shared-memory slots with cp.async.bulk.
+// One MMA tile is a pair of slice tiles: B = 128 real columns (64
+// determinants), so every tcgen05.mma is 128 x 128 x 16 (an MMA costs about
+// the same time at N = 64 and N = 128 here, so the wider tile halves the
+// contraction time per determinant).  The four level accumulators then fill
+// TMEM (4 x 128 columns) and are single-buffered.
+// Persistent, one CTA per SM, 18 warps: warps 0-15 epilogue (warp w reads TMEM
+// lanes 32 (w % 4) .. + 31 = pairs, columns 32 (w / 4) .. + 31 = 16
+// determinants), warp 16 TMEM allocation + MMA issue (lane 0), warp 17 lane 0
+// streams the slice images into a ring of shared-memory slots with
+// cp.async.bulk (one slot = up to four 16-column K chunks of both tiles).
 __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int KP = A.KP, R = A.ring;
   const uint32_t v_elems = (uint32_t)kM * KP;
-  const uint32_t slot_elems = (uint32_t)kChunkElems;
-  const uint32_t slot_bytes = slot_elems * 2u;
-  const int nch = KP / kChunkK;  // chunks per slice
+  const uint32_t slot_elems = (uint32_t)(kGroupK * kPairChunkElems);
+  const uint32_t pchunk_bytes = (uint32_t)kPairChunkElems * 2u;
+  const int nch = KP / kChunkK;                       // chunks per slice
+  const int ngr = (nch + kGroupK - 1) / kGroupK;      // ring slots per slice
+  const int64_t npairs = (A.ntiles + 1) / 2;
   __nv_bfloat16* sV = reinterpret_cast<__nv_bfloat16*>(smem);
   __nv_bfloat16* sD = sV + kSlices * v_elems;
   uint64_t* full = reinterpret_cast<uint64_t*>(sD + (size_t)R * slot_elems);
   uint64_t* empty = full + kMaxRing;
   uint64_t* accfull = empty + kMaxRing;
-  uint64_t* accempty = accfull + 2;
-  uint64_t* done = accempty + 2;
+  uint64_t* accempty = accfull + 1;
+  uint64_t* done = accempty + 1;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
 
@@ -319,10 +341,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       tc::mbar_init(&full[i], 1);
       tc::mbar_init(&empty[i], 1);
     }
-    for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(&accfull[i], 1);
-      tc::mbar_init(&accempty[i], kEpiWarps);
-    }
+    tc::mbar_init(accfull, 1);
+    tc::mbar_init(accempty, kEpiWarps);
     tc::mbar_init(done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -334,35 +354,44 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  // each CTA owns a contiguous run of tiles (consecutive tiles share an alpha
-  // row, so the G rows it writes are contiguous too)
-  const int64_t t_begin = A.ntiles * blockIdx.x / gridDim.x;
-  const int64_t t_end = A.ntiles * (blockIdx.x + 1) / gridDim.x;
+  // each CTA owns a contiguous run of tile pairs (consecutive tiles share an
+  // alpha row, so the G rows it writes are contiguous too)
+  const int64_t t_begin = npairs * blockIdx.x / gridDim.x;
+  const int64_t t_end = npairs * (blockIdx.x + 1) / gridDim.x;
 
   if (warp == kLoadWarp) {
     if (lane == 0) {
-      int64_t it = 0;
-      for (int64_t t = t_begin; t < t_end; ++t, ++it) {
-        const __nv_bfloat16* src = A.dslices + (size_t)t * kSlices * nch * slot_elems;
+      // ring position and phase advance incrementally (no 64-bit division)
+      int slot = 0;
+      uint32_t ph = 0;
+      for (int64_t t = t_begin; t < t_end; ++t) {
+        const __nv_bfloat16* src =
+            A.dslices + (size_t)t * kSlices * nch * kPairChunkElems;
         bool ok = true;
-        for (int b = 0; b < kSlices * nch; ++b) {
-          const int64_t g = it * kSlices * nch + b;
-          const int slot = (int)(g % R);
-          if (!oz_wait(&empty[slot], (uint32_t)(((g / R) & 1) ^ 1), abort_flag)) {
-            oz_abort(abort_flag, A.err, 5);
-            ok = false;
-            break;
+        for (int b = 0; b < kSlices && ok; ++b) {
+          for (int gi = 0; gi < ngr; ++gi) {
+            const int c0 = gi * kGroupK;
+            const uint32_t bytes = (uint32_t)min(kGroupK, nch - c0) * pchunk_bytes;
+            if (!oz_wait(&empty[slot], ph ^ 1u, abort_flag)) {
+              oz_abort(abort_flag, A.err, 5);
+              ok = false;
+              break;
+            }
+            tc::mbar_arrive_expect_tx(&full[slot], bytes);
+            tc::bulk_g2s(sD + (size_t)slot * slot_elems,
+                         src + ((size_t)b * nch + c0) * kPairChunkElems, bytes, &full[slot]);
+            if (++slot == R) {
+              slot = 0;
+              ph ^= 1u;
+            }
           }
-          tc::mbar_arrive_expect_tx(&full[slot], slot_bytes);
-          tc::bulk_g2s(sD + (size_t)slot * slot_elems, src + (size_t)b * slot_elems,
-                       slot_bytes, &full[slot]);
         }
         if (!ok) break;
       }
     }
   } else if (warp == kMmaWarp) {
     if (lane == 0) {
-      const uint32_t idesc = tc::make_idesc_bf16(kM, kN);
+      const uint32_t idesc = tc::make_idesc_bf16(kM, kNM);
       const uint32_t sbo = (uint32_t)KP * 16u;          // V: full-K rows
       const uint32_t sbo_c = (uint32_t)kChunkK * 16u;   // D chunk: 16-column rows
       // descriptors of k-step 0; k-step ks adds 256 bytes = 16 address units
@@ -370,24 +399,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       for (int a = 0; a < kSlices; ++a)
         adesc0[a] = tc::make_sdesc(tc::smem_u32(sV + (size_t)a * v_elems), 128, sbo);
       int64_t it = 0;
+      int slot = 0;
+      uint32_t ph = 0;
       for (int64_t t = t_begin; t < t_end; ++t, ++it) {
-        const int s = (int)(it & 1);
-        if (!oz_wait(&accempty[s], (uint32_t)(((it >> 1) & 1) ^ 1), abort_flag)) {
+        if (!oz_wait(accempty, (uint32_t)((it & 1) ^ 1), abort_flag)) {
           oz_abort(abort_flag, A.err, 2);
           break;
         }
         tc::fence_after_sync();
-        const uint32_t acc0 = tmem + (uint32_t)(s * kAccCols);
-        bool first[kAccs] = {true, true, true, true};
+        uint32_t fresh = (1u << kAccs) - 1u;  // accumulators not yet written
         bool ok = true;
-        // chunk (b, c): the 16 K columns c of D slice b; each is released as
-        // soon as its MMAs complete, so the loader runs many chunks ahead
+        // chunk group (b, gi): up to four 16-column K chunks of D slice b; a
+        // slot is released as soon as its MMAs complete
         for (int b = 1; b <= kSlices && ok; ++b) {
           const int amax = min(kSlices, kMaxLevel - b);
-          for (int c = 0; c < nch; ++c) {
-            const int64_t g = (it * kSlices + (b - 1)) * nch + c;
-            const int slot = (int)(g % R);
-            if (!oz_wait(&full[slot], (uint32_t)((g / R) & 1), abort_flag)) {
+          for (int gi = 0; gi < ngr; ++gi) {
+            const int c0 = gi * kGroupK;
+            const int nk = min(kGroupK, nch - c0);
+            if (!oz_wait(&full[slot], ph, abort_flag)) {
               oz_abort(abort_flag, A.err, 3);
               ok = false;
               break;
@@ -395,64 +424,82 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
             tc::fence_after_sync();
             const uint64_t bd =
                 tc::make_sdesc(tc::smem_u32(sD + (size_t)slot * slot_elems), 128, sbo_c);
-            for (int a = 1; a <= amax; ++a) {
-              const int lvl = a + b;
-              const int ai = lvl <= 4 ? lvl - 2 : 3;
-              const uint32_t acc = acc0 + (uint32_t)(ai * kN);
-              // A (V slice a) advances 256 bytes = 16 descriptor units per k-step
-              tc::mma_bf16(acc, adesc0[a - 1] + (uint64_t)(16 * c), bd, idesc,
-                           first[ai] ? 0u : 1u);
-              first[ai] = false;
+            // k-step outer, V slice inner: consecutive MMAs go to different
+            // accumulators (measured faster than runs into one accumulator)
+#pragma unroll
+            for (int c = 0; c < kGroupK; ++c) {
+              if (c < nk) {
+#pragma unroll
+                for (int a = 1; a <= kSlices; ++a) {
+                  if (a <= amax) {
+                    const int lvl = a + b;
+                    const int ai = lvl <= 4 ? lvl - 2 : 3;
+                    const uint32_t acc = tmem + (uint32_t)(ai * kNM);
+                    // A (V slice a) advances 256 bytes = 16 descriptor units per
+                    // k-step; B advances one 4 KB pair chunk = 256 units
+                    tc::mma_bf16(acc, adesc0[a - 1] + (uint64_t)(16 * (c0 + c)),
+                                 bd + (uint64_t)(256 * c), idesc,
+                                 (fresh >> ai) & 1u ? 0u : 1u);
+                    fresh &= ~(1u << ai);
+                  }
+                }
+              }
             }
             tc::mma_commit(&empty[slot]);
+            if (++slot == R) {
+              slot = 0;
+              ph ^= 1u;
+            }
           }
         }
         if (!ok) break;
-        tc::mma_commit(&accfull[s]);
+        tc::mma_commit(accfull);
       }
       // every MMA issued above has completed before TMEM is released
       tc::mma_commit(done);
       if (!oz_wait(done, 0, abort_flag) && !*abort_flag) oz_abort(abort_flag, A.err, 6);
     }
   } else {
-    const int quarter = warp & 3, half = warp >> 2;
+    const int quarter = warp & 3, cg = warp >> 2;
     const int p = 32 * quarter + lane;  // TMEM lane = pair row
     const int ev = (p < A.P) ? A.vexp[p] : 0;
     const int g0 = A.misc[0];
     const bool v8 = (A.lenb & 1) == 0;  // G rows start on 32-byte boundaries
+    const int dbase = (cg & 1) * 16;    // first determinant of this warp in its tile
     int64_t it = 0;
     for (int64_t t = t_begin; t < t_end; ++t, ++it) {
-      int64_t ia, ib0;
-      tile_coords(A, t, ia, ib0);
-      const int s = (int)(it & 1);
-      // exponents of the tile's 32 determinants: lane l holds determinant l
+      const int64_t ts = 2 * t + (cg >> 1);  // slice tile of this warp's columns
+      const bool live = ts < A.ntiles;
+      int64_t ia = 0, ib0 = 0;
+      if (live) tile_coords(A, ts, ia, ib0);
+      // exponents of the warp's 16 determinants: lane l < 16 holds determinant l
       uchar2 be_l = make_uchar2(0, 0);
-      if (ib0 + lane < A.lenb) be_l = A.bexp[ia * A.lenb + ib0 + lane];
+      if (live && lane < 16 && ib0 + dbase + lane < A.lenb)
+        be_l = A.bexp[ia * A.lenb + ib0 + dbase + lane];
       const int be_pack = (int)be_l.x | ((int)be_l.y << 8);
       const bool got = __all_sync(0xffffffffu,
-                                  oz_wait(&accfull[s], (uint32_t)((it >> 1) & 1), abort_flag));
+                                  oz_wait(accfull, (uint32_t)(it & 1), abort_flag));
       if (!got) {
         if (lane == 0) oz_abort(abort_flag, A.err, 4);
         break;
       }
       tc::fence_after_sync();
-      const uint32_t base =
-          tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(s * kAccCols);
-      float4* grow = A.G + ((int64_t)p * A.lena + ia) * A.lenb + ib0;
-      for (int c0 = 32 * half; c0 < 32 * half + 32; c0 += 16) {
-        uint32_t ra[16], rb[16], rc[16], rd[16];
-        tc::tmem_ld16_nowait(base + c0, ra);
-        tc::tmem_ld16_nowait(base + kN + c0, rb);
-        tc::tmem_ld16_nowait(base + 2 * kN + c0, rc);
-        tc::tmem_ld16_nowait(base + 3 * kN + c0, rd);
+      const uint32_t base = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(32 * cg);
+      float4* grow = A.G + ((int64_t)p * A.lena + ia) * A.lenb + ib0 + dbase;
+      for (int c0 = 0; c0 < 32; c0 += 8) {
+        uint32_t ra[8], rb[8], rc[8], rd[8];
+        tc::tmem_ld8_nowait(base + c0, ra);
+        tc::tmem_ld8_nowait(base + kNM + c0, rb);
+        tc::tmem_ld8_nowait(base + 2 * kNM + c0, rc);
+        tc::tmem_ld8_nowait(base + 3 * kNM + c0, rd);
         tc::tmem_wait_ld();
-        int bes[8];
+        int bes[4];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) bes[k] = __shfl_sync(0xffffffffu, be_pack, c0 / 2 + k);
-        if (p >= A.P) continue;
-        float out[8][4];  // determinants c0/2 .. c0/2 + 7: re hi, re lo, im hi, im lo
+        for (int k = 0; k < 4; ++k) bes[k] = __shfl_sync(0xffffffffu, be_pack, c0 / 2 + k);
+        if (p >= A.P || !live) continue;
+        float out[4][4];  // determinants c0/2 .. c0/2 + 3: re hi, re lo, im hi, im lo
 #pragma unroll
-        for (int j = 0; j < 16; j += 2) {
+        for (int j = 0; j < 8; j += 2) {
 #pragma unroll
           for (int part = 0; part < 2; ++part) {
             // column exponent: |D| < 2^(bits - 62 + g0)
@@ -478,11 +525,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
           }
         }
         const int d0 = c0 / 2;
-        if (v8 && ib0 + d0 + 8 <= A.lenb) {
-          // full 32-byte sectors: two determinants per store (row start and
-          // d0 are even, lenb is even, so every address is 32-byte aligned)
+        if (v8 && ib0 + dbase + d0 + 4 <= A.lenb) {
+          // full 32-byte sectors: two determinants per store (row start, ib0,
+          // dbase and d0 are even and lenb is even: 32-byte aligned)
 #pragma unroll
-          for (int k = 0; k < 8; k += 2) {
+          for (int k = 0; k < 4; k += 2) {
             float* q = reinterpret_cast<float*>(grow + d0 + k);
             asm volatile(
                 "st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(q),
@@ -492,14 +539,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
           }
         } else {
 #pragma unroll
-          for (int k = 0; k < 8; ++k)
-            if (ib0 + d0 + k < A.lenb)
+          for (int k = 0; k < 4; ++k)
+            if (ib0 + dbase + d0 + k < A.lenb)
               grow[d0 + k] = make_float4(out[k][0], out[k][1], out[k][2], out[k][3]);
         }
       }
       tc::fence_before_sync();
       __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&accempty[s]);
+      if (lane == 0) tc::mbar_arrive(accempty);
     }
   }
   tc::fence_before_sync();
@@ -664,8 +711,10 @@ static int plan_create(fqegpu_ham h) {
   FQE_CUDA(cudaMalloc(&pl->d_G, sizeof(float4) * (size_t)P * N));
   FQE_CUDA(cudaMalloc(&pl->d_bexp, sizeof(uchar2) * N));
   const int64_t ntiles = lena * ((lenb + kDets - 1) / kDets);
-  FQE_CUDA(cudaMalloc(&pl->d_dslices,
-                      sizeof(__nv_bfloat16) * (size_t)ntiles * kSlices * kN * KP));
+  const int64_t npairs = (ntiles + 1) / 2;
+  const size_t dsl = sizeof(__nv_bfloat16) * (size_t)npairs * 2 * kSlices * kN * KP;
+  FQE_CUDA(cudaMalloc(&pl->d_dslices, dsl));
+  FQE_CUDA(cudaMemset(pl->d_dslices, 0, dsl));  // the unpaired last tile reads zeros
   int dev = 0;
   FQE_CUDA(cudaGetDevice(&dev));
   FQE_CUDA(cudaDeviceGetAttribute(&pl->nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -673,10 +722,10 @@ static int plan_create(fqegpu_ham h) {
   int smax = 0;
   FQE_CUDA(cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const size_t fixed = sizeof(__nv_bfloat16) * (size_t)kSlices * vel +
-                       sizeof(uint64_t) * (2 * kMaxRing + 5) + 16;
-  const size_t slot = sizeof(__nv_bfloat16) * (size_t)kChunkElems;
+                       sizeof(uint64_t) * (2 * kMaxRing + 3) + 16;
+  const size_t slot = sizeof(__nv_bfloat16) * (size_t)kGroupK * kPairChunkElems;
   pl->ring = (int)std::min<size_t>(kMaxRing, ((size_t)smax - fixed) / slot);
-  if (pl->ring < 2 * kSlices) {
+  if (pl->ring < 2) {
     set_error("shared memory too small for the tensor-core contraction");
     return FQEGPU_ERR_UNSUPPORTED;
   }
@@ -746,7 +795,7 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   k_oz_slice<<<(unsigned)A.ntiles, kSliceThreads, 0, st>>>(A);
   FQE_CUDA(cudaGetLastError());
   FQE_TRY(stage_mark(h, 0, 1, st));
-  const int grid = (int)std::min<int64_t>(pl->nsm, A.ntiles);
+  const int grid = (int)std::min<int64_t>(pl->nsm, (A.ntiles + 1) / 2);
   k_oz_mma<<<grid, kThreads, pl->smem, st>>>(A);
   FQE_CUDA(cudaGetLastError());
   FQE_TRY(stage_mark(h, 0, 2, st));
