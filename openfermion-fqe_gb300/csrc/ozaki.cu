@@ -84,6 +84,8 @@ struct OzakiPlan {
   int32_t* d_misc = nullptr;           // [0] = global exponent, [1] = error
   float4* d_G = nullptr;               // [P][N]
   uchar2* d_bexp = nullptr;            // [N]
+  int32_t* d_tabTA = nullptr;          // [lena][KP] target tables, pair index fastest
+  int32_t* d_tabTB = nullptr;          // [lenb][KP]
   __nv_bfloat16* d_dslices = nullptr;  // [ntiles][5][64 * KP] smem images
   int ring = 0;
   int nsm = 0;
@@ -96,6 +98,8 @@ struct OzArgs {
   int nb;  // column blocks per row
   const int32_t* tabA;
   const int32_t* tabB;
+  const int32_t* tabTA;  // [lena][KP]: the 8 pairs of an octet are 32 contiguous bytes
+  const int32_t* tabTB;  // [lenb][KP]
   const longlong2* psix;
   const int32_t* misc;
   const __nv_bfloat16* vslices;
@@ -158,16 +162,13 @@ __device__ __forceinline__ uint64_t round40(uint64_t m, int sh) {
   return r > cap ? cap : r;
 }
 
-// D[q][det] (real and imaginary part) in 62-bit fixed point: the alpha and
-// beta sources of the pair q through the target tables.
-__device__ __forceinline__ void gather_d(const OzArgs& A, int q, bool live, uint32_t ia,
-                                         uint32_t ib, uint32_t lena, uint32_t lenb,
-                                         long long& re, long long& im) {
+// D[q][det] (real and imaginary part) in 62-bit fixed point from the alpha
+// and beta target-table entries ca, cb of the pair q (0: no source).
+__device__ __forceinline__ void gather_d(const OzArgs& A, int32_t ca, int32_t cb, uint32_t ia,
+                                         uint32_t ib, uint32_t lenb, long long& re,
+                                         long long& im) {
   re = 0;
   im = 0;
-  if (!live || q >= A.P) return;
-  const int32_t ca = __ldg(A.tabA + (uint32_t)q * lena + ia);
-  const int32_t cb = __ldg(A.tabB + (uint32_t)q * lenb + ib);
   if (ca) {
     const longlong2 x = __ldg(A.psix + ((uint32_t)(abs(ca) - 1) * lenb + ib));
     if (ca > 0) { re += x.x; im += x.y; } else { re -= x.x; im -= x.y; }
@@ -226,7 +227,7 @@ __global__ void __launch_bounds__(kSliceThreads, 2) k_oz_slice(OzArgs A) {
   const int64_t t = blockIdx.x;
   int64_t ia64, ib064;
   tile_coords(A, t, ia64, ib064);
-  const uint32_t lena32 = (uint32_t)A.lena, lenb32 = (uint32_t)A.lenb;
+  const uint32_t lenb32 = (uint32_t)A.lenb;
   const uint32_t ia = (uint32_t)ia64;
   const int d = 4 * grp + (lane & 3);
   const uint32_t ib = (uint32_t)ib064 + d;
@@ -237,10 +238,22 @@ __global__ void __launch_bounds__(kSliceThreads, 2) k_oz_slice(OzArgs A) {
   uint64_t mre[8], mim[8];
   uint32_t nre = 0u, nim = 0u;
   int blr = 0, bli = 0;
+  // the octet's eight table entries per spin: two 16-byte loads each
+  int4 ta0 = make_int4(0, 0, 0, 0), ta1 = ta0, tb0 = ta0, tb1 = ta0;
+  if (live) {
+    const int4* pa = reinterpret_cast<const int4*>(A.tabTA + (size_t)ia * KP + 8 * o);
+    const int4* pb = reinterpret_cast<const int4*>(A.tabTB + (size_t)ib * KP + 8 * o);
+    ta0 = __ldg(pa);
+    ta1 = __ldg(pa + 1);
+    tb0 = __ldg(pb);
+    tb1 = __ldg(pb + 1);
+  }
+  const int32_t cas[8] = {ta0.x, ta0.y, ta0.z, ta0.w, ta1.x, ta1.y, ta1.z, ta1.w};
+  const int32_t cbs[8] = {tb0.x, tb0.y, tb0.z, tb0.w, tb1.x, tb1.y, tb1.z, tb1.w};
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     long long re, im;
-    gather_d(A, 8 * o + j, live, ia, ib, lena32, lenb32, re, im);
+    gather_d(A, cas[j], cbs[j], ia, ib, lenb32, re, im);
     nre |= (re < 0 ? 1u : 0u) << j;
     nim |= (im < 0 ? 1u : 0u) << j;
     mre[j] = (uint64_t)(re < 0 ? -re : re);
@@ -666,6 +679,16 @@ __global__ void __launch_bounds__(256) k_oz_scatter(
   sigma[I] = out;
 }
 
+// tabT[s][q] = tab[q][s] for q < P, 0 for P <= q < KP.
+__global__ void k_oz_transpose_tab(int P, int KP, int64_t len, const int32_t* __restrict__ tab,
+                                   int32_t* __restrict__ tabT) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= len * KP) return;
+  const int64_t s = i / KP;
+  const int q = (int)(i - s * KP);
+  tabT[i] = q < P ? tab[(int64_t)q * len + s] : 0;
+}
+
 // ---- host ---------------------------------------------------------------------
 static int plan_create(fqegpu_ham h) {
   auto* pl = new (std::nothrow) OzakiPlan();
@@ -710,6 +733,19 @@ static int plan_create(fqegpu_ham h) {
   FQE_CUDA(cudaMalloc(&pl->d_misc, sizeof(int32_t) * 4));
   FQE_CUDA(cudaMalloc(&pl->d_G, sizeof(float4) * (size_t)P * N));
   FQE_CUDA(cudaMalloc(&pl->d_bexp, sizeof(uchar2) * N));
+  {
+    const bool tri = h->compressed;
+    const int32_t* ta = tri ? h->g->a.tab_tri : h->g->a.tab_full;
+    const int32_t* tb = tri ? h->g->b.tab_tri : h->g->b.tab_full;
+    FQE_CUDA(cudaMalloc(&pl->d_tabTA, sizeof(int32_t) * (size_t)lena * KP));
+    FQE_CUDA(cudaMalloc(&pl->d_tabTB, sizeof(int32_t) * (size_t)lenb * KP));
+    k_oz_transpose_tab<<<(unsigned)((lena * KP + 255) / 256), 256>>>(P, KP, lena, ta,
+                                                                     pl->d_tabTA);
+    k_oz_transpose_tab<<<(unsigned)((lenb * KP + 255) / 256), 256>>>(P, KP, lenb, tb,
+                                                                     pl->d_tabTB);
+    FQE_CUDA(cudaGetLastError());
+    FQE_CUDA(cudaDeviceSynchronize());
+  }
   const int64_t ntiles = lena * ((lenb + kDets - 1) / kDets);
   const int64_t npairs = (ntiles + 1) / 2;
   const size_t dsl = sizeof(__nv_bfloat16) * (size_t)npairs * 2 * kSlices * kN * KP;
@@ -745,6 +781,8 @@ void ozaki_destroy(fqegpu_ham h) {
   cudaFree(pl->d_misc);
   cudaFree(pl->d_G);
   cudaFree(pl->d_bexp);
+  cudaFree(pl->d_tabTA);
+  cudaFree(pl->d_tabTB);
   cudaFree(pl->d_dslices);
   delete pl;
   h->oz = nullptr;
@@ -790,6 +828,8 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   A.vexp = pl->d_vexp;
   A.G = pl->d_G;
   A.bexp = pl->d_bexp;
+  A.tabTA = pl->d_tabTA;
+  A.tabTB = pl->d_tabTB;
   A.dslices = pl->d_dslices;
   A.err = pl->d_misc + 1;
   k_oz_slice<<<(unsigned)A.ntiles, kSliceThreads, 0, st>>>(A);
