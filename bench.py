@@ -313,11 +313,22 @@ def run_gpu(args):
                     "peak": hbm_peak},
     }
     dk = stages[names[dom]]
+    traffic = None
+    if prec == "ozaki" and names[dom] == "contraction":
+        # k_oz_mma DRAM bytes per launch: a full ncu capture of the same kernel
+        # at norb 12 measured 0.98 x its algorithmic bytes (slice images read
+        # once, G written once); scaled to this workload's algorithmic bytes
+        ntiles = d.lena() * ((d.lenb() + 31) // 32)
+        images = 2 * ((ntiles + 1) // 2) * 5 * 64 * KP * 2.0
+        traffic = 0.98 * (images + 16.0 * P * n)
     roofline = {"kernel": names[dom], "bound": dk["bound"],
                 "achieved": dk["achieved"], "peak": dk["peak"],
                 "unit": dk["unit"],
                 "frac": (dk["achieved"] / dk["peak"]) if dk["achieved"] else None,
-                "traffic": None, "peak_source": peak_src if dk["bound"] != "fp64"
+                "traffic": traffic,
+                "traffic_source": "ncu capture at norb 12 scaled by algorithmic bytes"
+                if traffic else None,
+                "peak_source": peak_src if dk["bound"] != "fp64"
                 else "torch float64 matmul 4096^3 on a GB300 of this pool"}
     # whole-apply HBM view with the uncompressed dvec byte model 16 norb^2 + 32
     alg_bytes = (16.0 * NORB * NORB + 32.0) * n
