@@ -313,20 +313,23 @@ __global__ void __launch_bounds__(kSliceThreads, 2) k_oz_slice(OzArgs A) {
 }
 
 // ---- contraction: bulk-copied slices, tcgen05 MMAs, TMEM epilogue -----------
-// One MMA tile is a pair of slice tiles: B = 128 real columns (64
-// determinants), so every tcgen05.mma is 128 x 128 x 16 (an MMA costs about
-// the same time at N = 64 and N = 128 here, so the wider tile halves the
-// contraction time per determinant).  The four level accumulators then fill
-// TMEM (4 x 128 columns) and are single-buffered.
+// One MMA tile is a pair of slice tiles: 64 determinants = 128 real rows.  The
+// MMA is G^T = D^T V^T: A = a 128-row K chunk of D slice b (streamed), B = V
+// slice a (KP rows = pairs, resident), D in TMEM = 128 lanes (determinant,
+// real/imaginary) x KP columns (pairs) per level accumulator (4 x KP <= 512
+// columns, single-buffered).  An MMA costs about the same time at N = 64 and
+// N = 128 here, so covering 64 determinants per instruction halves the
+// contraction time per determinant; with lanes = determinants the epilogue's
+// G stores are coalesced (a warp writes 16 determinants x 16 B of one pair).
 // Persistent, one CTA per SM, 18 warps: warps 0-15 epilogue (warp w reads TMEM
-// lanes 32 (w % 4) .. + 31 = pairs, columns 32 (w / 4) .. + 31 = 16
-// determinants), warp 16 TMEM allocation + MMA issue (lane 0), warp 17 lane 0
-// streams the slice images into a ring of shared-memory slots with
-// cp.async.bulk (one slot = up to four 16-column K chunks of both tiles).
+// lanes 32 (w % 4) .. + 31 = 16 determinants of one slice tile, columns = the
+// pairs of group w / 4), warp 16 TMEM allocation + MMA issue (lane 0), warp 17
+// lane 0 streams the slice images into a ring of shared-memory slots with
+// cp.async.bulk (one slot = up to four 16-column K chunks of a tile pair).
 __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int KP = A.KP, R = A.ring;
-  const uint32_t v_elems = (uint32_t)kM * KP;
+  const uint32_t v_elems = (uint32_t)KP * KP;
   const uint32_t slot_elems = (uint32_t)(kGroupK * kPairChunkElems);
   const uint32_t pchunk_bytes = (uint32_t)kPairChunkElems * 2u;
   const int nch = KP / kChunkK;                       // chunks per slice
@@ -341,6 +344,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   uint64_t* done = accempty + 1;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+  int* sVexp = reinterpret_cast<int*>(tslot + 2);  // [kM] row exponents of V
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   {
@@ -348,6 +352,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
     int4* dst = reinterpret_cast<int4*>(sV);
     const int n16 = (int)(kSlices * v_elems * 2 / 16);
     for (int i = tid; i < n16; i += blockDim.x) dst[i] = src[i];
+    for (int i = tid; i < kM; i += blockDim.x) sVexp[i] = A.vexp[i];
   }
   if (tid == 0) {
     for (int i = 0; i < R; ++i) {
@@ -404,13 +409,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
     }
   } else if (warp == kMmaWarp) {
     if (lane == 0) {
-      const uint32_t idesc = tc::make_idesc_bf16(kM, kNM);
+      const uint32_t idesc = tc::make_idesc_bf16(kM, (uint32_t)KP);
       const uint32_t sbo = (uint32_t)KP * 16u;          // V: full-K rows
       const uint32_t sbo_c = (uint32_t)kChunkK * 16u;   // D chunk: 16-column rows
-      // descriptors of k-step 0; k-step ks adds 256 bytes = 16 address units
-      uint64_t adesc0[kSlices];
+      // B = V slice descriptors of k-step 0; k-step ks adds 256 bytes = 16 units
+      uint64_t vdesc0[kSlices];
       for (int a = 0; a < kSlices; ++a)
-        adesc0[a] = tc::make_sdesc(tc::smem_u32(sV + (size_t)a * v_elems), 128, sbo);
+        vdesc0[a] = tc::make_sdesc(tc::smem_u32(sV + (size_t)a * v_elems), 128, sbo);
       int64_t it = 0;
       int slot = 0;
       uint32_t ph = 0;
@@ -435,7 +440,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
               break;
             }
             tc::fence_after_sync();
-            const uint64_t bd =
+            const uint64_t dd =
                 tc::make_sdesc(tc::smem_u32(sD + (size_t)slot * slot_elems), 128, sbo_c);
             // k-step outer, V slice inner: consecutive MMAs go to different
             // accumulators (measured faster than runs into one accumulator)
@@ -447,11 +452,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
                   if (a <= amax) {
                     const int lvl = a + b;
                     const int ai = lvl <= 4 ? lvl - 2 : 3;
-                    const uint32_t acc = tmem + (uint32_t)(ai * kNM);
-                    // A (V slice a) advances 256 bytes = 16 descriptor units per
-                    // k-step; B advances one 4 KB pair chunk = 256 units
-                    tc::mma_bf16(acc, adesc0[a - 1] + (uint64_t)(16 * (c0 + c)),
-                                 bd + (uint64_t)(256 * c), idesc,
+                    const uint32_t acc = tmem + (uint32_t)(ai * KP);
+                    // A (D chunk) advances one 4 KB pair chunk = 256 units per
+                    // k-step; B (V slice a) advances 256 bytes = 16 units
+                    tc::mma_bf16(acc, dd + (uint64_t)(256 * c),
+                                 vdesc0[a - 1] + (uint64_t)(16 * (c0 + c)), idesc,
                                  (fresh >> ai) & 1u ? 0u : 1u);
                     fresh &= ~(1u << ai);
                   }
@@ -474,22 +479,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
     }
   } else {
     const int quarter = warp & 3, cg = warp >> 2;
-    const int p = 32 * quarter + lane;  // TMEM lane = pair row
-    const int ev = (p < A.P) ? A.vexp[p] : 0;
+    const int row = 32 * quarter + lane;      // TMEM lane = MMA row
+    const int half = row >> 6;                // slice tile of the pair
+    const int det = (row & 63) >> 1;          // determinant in that tile
+    const int part = row & 1;                 // 0 real, 1 imaginary
+    const int cw = KP / 4;                    // pairs per column group
+    const int pbeg = cg * cw;
     const int g0 = A.misc[0];
-    const bool v8 = (A.lenb & 1) == 0;  // G rows start on 32-byte boundaries
-    const int dbase = (cg & 1) * 16;    // first determinant of this warp in its tile
     int64_t it = 0;
     for (int64_t t = t_begin; t < t_end; ++t, ++it) {
-      const int64_t ts = 2 * t + (cg >> 1);  // slice tile of this warp's columns
-      const bool live = ts < A.ntiles;
+      const int64_t ts = 2 * t + half;
+      const bool live_tile = ts < A.ntiles;
       int64_t ia = 0, ib0 = 0;
-      if (live) tile_coords(A, ts, ia, ib0);
-      // exponents of the warp's 16 determinants: lane l < 16 holds determinant l
-      uchar2 be_l = make_uchar2(0, 0);
-      if (live && lane < 16 && ib0 + dbase + lane < A.lenb)
-        be_l = A.bexp[ia * A.lenb + ib0 + dbase + lane];
-      const int be_pack = (int)be_l.x | ((int)be_l.y << 8);
+      if (live_tile) tile_coords(A, ts, ia, ib0);
+      const int64_t ib = ib0 + det;
+      const bool live = live_tile && ib < A.lenb;
+      int bits = 0;
+      if (live) {
+        const uchar2 be = A.bexp[ia * A.lenb + ib];
+        bits = part ? be.y : be.x;
+      }
       const bool got = __all_sync(0xffffffffu,
                                   oz_wait(accfull, (uint32_t)(it & 1), abort_flag));
       if (!got) {
@@ -497,64 +506,42 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
         break;
       }
       tc::fence_after_sync();
-      const uint32_t base = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(32 * cg);
-      float4* grow = A.G + ((int64_t)p * A.lena + ia) * A.lenb + ib0 + dbase;
-      for (int c0 = 0; c0 < 32; c0 += 8) {
-        uint32_t ra[8], rb[8], rc[8], rd[8];
-        tc::tmem_ld8_nowait(base + c0, ra);
-        tc::tmem_ld8_nowait(base + kNM + c0, rb);
-        tc::tmem_ld8_nowait(base + 2 * kNM + c0, rc);
-        tc::tmem_ld8_nowait(base + 3 * kNM + c0, rd);
+      const uint32_t base = tmem + ((uint32_t)(32 * quarter) << 16);
+      // this lane's half of G[p][det]: (hi, lo) of the real or imaginary part
+      float2* gcol = reinterpret_cast<float2*>(A.G + ia * A.lenb + ib) + part;
+      const int64_t pstride = A.lena * A.lenb * 2;  // float2 elements per pair row
+      for (int c0 = 0; c0 < cw; c0 += 4) {
+        const int pc = pbeg + c0;
+        uint32_t ra[4], rb[4], rc[4], rd[4];
+        tc::tmem_ld4_nowait(base + (uint32_t)pc, ra);
+        tc::tmem_ld4_nowait(base + (uint32_t)(KP + pc), rb);
+        tc::tmem_ld4_nowait(base + (uint32_t)(2 * KP + pc), rc);
+        tc::tmem_ld4_nowait(base + (uint32_t)(3 * KP + pc), rd);
         tc::tmem_wait_ld();
-        int bes[4];
+        if (!live) continue;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) bes[k] = __shfl_sync(0xffffffffu, be_pack, c0 / 2 + k);
-        if (p >= A.P || !live) continue;
-        float out[4][4];  // determinants c0/2 .. c0/2 + 3: re hi, re lo, im hi, im lo
-#pragma unroll
-        for (int j = 0; j < 8; j += 2) {
-#pragma unroll
-          for (int part = 0; part < 2; ++part) {
-            // column exponent: |D| < 2^(bits - 62 + g0)
-            const int bits = part ? (bes[j / 2] >> 8) : (bes[j / 2] & 0xFF);
-            const int sc = ev + bits - 62 + g0;
-            const float x = __uint_as_float(ra[j + part]), y = __uint_as_float(rb[j + part]);
-            // exact two-sum of levels 2 and 3, then levels 4 and 5..7
-            const float h = x + y;
-            const float bb = h - x;
-            float l = (x - (h - bb)) + (y - bb);
-            l += __uint_as_float(rc[j + part]);
-            l += __uint_as_float(rd[j + part]);
-            const float h2 = h + l;
-            const float l2 = l - (h2 - h);
-            if (sc >= -126 && sc <= 127) {
-              const float f = pow2f(sc);
-              out[j / 2][2 * part] = h2 * f;
-              out[j / 2][2 * part + 1] = l2 * f;
-            } else {
-              out[j / 2][2 * part] = scale2(h2, sc);
-              out[j / 2][2 * part + 1] = scale2(l2, sc);
-            }
+        for (int k = 0; k < 4; ++k) {
+          const int p = pc + k;
+          if (p >= A.P) break;
+          // column exponent: |D| < 2^(bits - 62 + g0); row exponent of V
+          const int sc = sVexp[p] + bits - 62 + g0;
+          const float x = __uint_as_float(ra[k]), y = __uint_as_float(rb[k]);
+          // exact two-sum of levels 2 and 3, then levels 4 and 5..7
+          const float h = x + y;
+          const float bb = h - x;
+          float l = (x - (h - bb)) + (y - bb);
+          l += __uint_as_float(rc[k]);
+          l += __uint_as_float(rd[k]);
+          const float h2 = h + l;
+          const float l2 = l - (h2 - h);
+          float2 o;
+          if (sc >= -126 && sc <= 127) {
+            const float f = pow2f(sc);
+            o = make_float2(h2 * f, l2 * f);
+          } else {
+            o = make_float2(scale2(h2, sc), scale2(l2, sc));
           }
-        }
-        const int d0 = c0 / 2;
-        if (v8 && ib0 + dbase + d0 + 4 <= A.lenb) {
-          // full 32-byte sectors: two determinants per store (row start, ib0,
-          // dbase and d0 are even and lenb is even: 32-byte aligned)
-#pragma unroll
-          for (int k = 0; k < 4; k += 2) {
-            float* q = reinterpret_cast<float*>(grow + d0 + k);
-            asm volatile(
-                "st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(q),
-                "f"(out[k][0]), "f"(out[k][1]), "f"(out[k][2]), "f"(out[k][3]),
-                "f"(out[k + 1][0]), "f"(out[k + 1][1]), "f"(out[k + 1][2]), "f"(out[k + 1][3])
-                : "memory");
-          }
-        } else {
-#pragma unroll
-          for (int k = 0; k < 4; ++k)
-            if (ib0 + dbase + d0 + k < A.lenb)
-              grow[d0 + k] = make_float4(out[k][0], out[k][1], out[k][2], out[k][3]);
+          gcol[(int64_t)p * pstride] = o;
         }
       }
       tc::fence_before_sync();
@@ -701,7 +688,7 @@ static int plan_create(fqegpu_ham h) {
   const int KP = (P + 15) / 16 * 16;
   pl->P = P;
   pl->KP = KP;
-  const size_t vel = (size_t)kM * KP;
+  const size_t vel = (size_t)KP * KP;  // V slice: KP rows (pairs) x KP
   std::vector<__nv_bfloat16> sl(kSlices * vel, __float2bfloat16(0.0f));
   std::vector<int32_t> vexp(kM, 0);
   for (int p = 0; p < P; ++p) {
@@ -758,7 +745,7 @@ static int plan_create(fqegpu_ham h) {
   int smax = 0;
   FQE_CUDA(cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const size_t fixed = sizeof(__nv_bfloat16) * (size_t)kSlices * vel +
-                       sizeof(uint64_t) * (2 * kMaxRing + 3) + 16;
+                       sizeof(uint64_t) * (2 * kMaxRing + 3) + 16 + sizeof(int) * kM;
   const size_t slot = sizeof(__nv_bfloat16) * (size_t)kGroupK * kPairChunkElems;
   pl->ring = (int)std::min<size_t>(kMaxRing, ((size_t)smax - fixed) / slot);
   if (pl->ring < 2) {
