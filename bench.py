@@ -282,7 +282,7 @@ def run_gpu(args):
     lena = d.lena()
     hbm_peak, bf16_peak, peak_src = peaks()
     flops_fp64_peak = 1.10  # TFLOP/s, GB300 DGEMM probed with torch on this machine
-    # algorithmic work per apply (contraction 2 real GEMMs of
+    # algorithmic work per apply (contraction: 2 real GEMMs of
     # P x P x N; gather writes and scatter reads D/G at 16 B per element)
     KP = (P + 15) // 16 * 16
     if prec == "ozaki":

@@ -124,8 +124,9 @@ int fqegpu_apply(fqegpu_ham h, const double *d_psi, double *d_sigma,
                  double alpha_re, double alpha_im, double beta_re,
                  double beta_im, int precision, void *stream);
 /* Same with host buffers: copies psi in and sigma out (pageable or pinned),
- * synchronous.  This is the call a ctypes binding inside the reference's
- * FqeData would make. */
+ * synchronous; the device staging buffer is allocated on the first call and
+ * kept by the handle.  This is the call a ctypes binding inside the
+ * reference's FqeData would make. */
 int fqegpu_apply_host(fqegpu_ham h, const double *h_psi, double *h_sigma,
                       double alpha_re, double alpha_im, double beta_re,
                       double beta_im, int precision);
@@ -180,6 +181,16 @@ int fqegpu_vdot(int64_t n, const double *d_x, const double *d_y,
                 double *h_result2, void *stream);
 int fqegpu_norm2(int64_t n, const double *d_x, double *h_result,
                  void *stream);
+/* Block forms for a Davidson subspace (no counterpart in the reference, whose
+ * Davidson works on dense numpy matrices, algorithm/davidson.py:186-268):
+ *   h_out[2i..2i+1] = <V_i | t>,  i < k   (one synchronisation for all k)
+ *   d_t += sum_i c_i V_i                   (one pass over d_t)
+ * h_vecs: host array of k device pointers to complex128[n]; k <= 64;
+ * h_coef: complex128[k] on the host.  Deterministic. */
+int fqegpu_block_vdot(int64_t n, int k, const double *const *h_vecs,
+                      const double *d_t, double *h_out, void *stream);
+int fqegpu_block_axpy(int64_t n, int k, const double *h_coef,
+                      const double *const *h_vecs, double *d_t, void *stream);
 
 /* ---- A10: Taylor propagator ------------------------------------------------
  * d_psi <- sum_k (-i t H)^k / k! d_psi until ||term|| < accuracy, at most

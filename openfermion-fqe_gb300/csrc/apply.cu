@@ -597,8 +597,11 @@ extern "C" int fqegpu_apply_host(fqegpu_ham h, const double* h_psi,
   clear_error();
   FQE_CHECK_ARG(h && h_psi && h_sigma, "NULL handle or buffer");
   const int64_t N = h->g->a.len * h->g->b.len;
-  double2* d = nullptr;
-  FQE_CUDA(cudaMalloc(&d, sizeof(double2) * 2 * N));
+  // device staging: the handle's two-vector work buffer (also the Taylor
+  // workspace), allocated once and kept, so a call costs the two copies and
+  // the apply
+  if (!h->d_vec) FQE_CUDA(cudaMalloc(&h->d_vec, sizeof(double2) * 2 * (size_t)N));
+  double2* d = h->d_vec;
   int s = FQEGPU_OK;
   cudaError_t e = cudaMemcpy(d, h_psi, sizeof(double2) * N, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {
@@ -607,7 +610,6 @@ extern "C" int fqegpu_apply_host(fqegpu_ham h, const double* h_psi,
     if (s == FQEGPU_OK)
       e = cudaMemcpy(h_sigma, d + N, sizeof(double2) * N, cudaMemcpyDeviceToHost);
   }
-  cudaFree(d);
   if (e != cudaSuccess) {
     set_error("apply_host: %s", cudaGetErrorString(e));
     return FQEGPU_ERR_CUDA;

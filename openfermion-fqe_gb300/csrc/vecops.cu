@@ -147,6 +147,76 @@ static int dot_host(int64_t n, const double2* x, const double2* y, double2* h,
   return s;
 }
 
+// ---- block operations (Davidson Gram-Schmidt and Ritz vectors) -----------------
+constexpr int kBlockMax = 64;
+struct VecPtrs {
+  const double2* p[kBlockMax];
+};
+struct Coefs {
+  double2 c[kBlockMax];
+};
+constexpr int kBlockDotParts = 256;
+
+// partial[i * gridDim.x + b] = block b's share of conj(V_i) t  (grid.y = i)
+__global__ void k_block_dot_partial(int64_t n, VecPtrs V, const double2* __restrict__ t,
+                                    double2* __restrict__ partial) {
+  __shared__ double2 sh[kRedThreads];
+  const double2* __restrict__ x = V.p[blockIdx.y];
+  double re = 0.0, im = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 a = x[i], b = t[i];
+    re += a.x * b.x + a.y * b.y;
+    im += a.x * b.y - a.y * b.x;
+  }
+  sh[threadIdx.x] = make_double2(re, im);
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sh[threadIdx.x].x += sh[threadIdx.x + s].x;
+      sh[threadIdx.x].y += sh[threadIdx.x + s].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] = sh[0];
+}
+
+// out[i] = sum over b of partial[i][b] in a fixed order (one block per i)
+__global__ void k_block_dot_final(int nparts, const double2* __restrict__ partial,
+                                  double2* __restrict__ out) {
+  __shared__ double2 sh[kRedThreads];
+  const double2* p = partial + (int64_t)blockIdx.x * nparts;
+  double re = 0.0, im = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+    re += p[i].x;
+    im += p[i].y;
+  }
+  sh[threadIdx.x] = make_double2(re, im);
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sh[threadIdx.x].x += sh[threadIdx.x + s].x;
+      sh[threadIdx.x].y += sh[threadIdx.x + s].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+}
+
+// t += sum_i c_i V_i, one pass over t
+__global__ void k_block_axpy(int64_t n, int k, VecPtrs V, Coefs c, double2* __restrict__ t) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    double2 acc = t[j];
+    for (int i = 0; i < k; ++i) {
+      const double2 v = V.p[i][j];
+      acc.x += c.c[i].x * v.x - c.c[i].y * v.y;
+      acc.y += c.c[i].x * v.y + c.c[i].y * v.x;
+    }
+    t[j] = acc;
+  }
+}
+
 }  // namespace fqegpu
 
 using namespace fqegpu;
@@ -201,5 +271,56 @@ extern "C" int fqegpu_norm2(int64_t n, const double* d_x, double* h_result,
   double2 r;
   FQE_TRY(dot_host(n, (const double2*)d_x, nullptr, &r, (cudaStream_t)stream));
   *h_result = sqrt(r.x);
+  return FQEGPU_OK;
+}
+
+extern "C" int fqegpu_block_vdot(int64_t n, int k, const double* const* h_vecs,
+                                 const double* d_t, double* h_out, void* stream) {
+  clear_error();
+  FQE_CHECK_ARG(n >= 0 && k >= 0 && k <= kBlockMax && d_t && h_out && (k == 0 || h_vecs),
+                "bad block_vdot arguments (at most 64 vectors)");
+  if (k == 0) return FQEGPU_OK;
+  VecPtrs V;
+  for (int i = 0; i < k; ++i) {
+    FQE_CHECK_ARG(h_vecs[i], "NULL vector");
+    V.p[i] = (const double2*)h_vecs[i];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  double2* scratch = nullptr;
+  FQE_CUDA(cudaMallocAsync(&scratch, sizeof(double2) * (size_t)k * (kBlockDotParts + 1), st));
+  double2* d_out = scratch + (size_t)k * kBlockDotParts;
+  k_block_dot_partial<<<dim3(kBlockDotParts, k), kRedThreads, 0, st>>>(
+      n, V, (const double2*)d_t, scratch);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    k_block_dot_final<<<k, kRedThreads, 0, st>>>(kBlockDotParts, scratch, d_out);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h_out, d_out, sizeof(double2) * k, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFreeAsync(scratch, st);
+  if (e != cudaSuccess) {
+    set_error("block_vdot: %s", cudaGetErrorString(e));
+    return FQEGPU_ERR_CUDA;
+  }
+  return FQEGPU_OK;
+}
+
+extern "C" int fqegpu_block_axpy(int64_t n, int k, const double* h_coef,
+                                 const double* const* h_vecs, double* d_t, void* stream) {
+  clear_error();
+  FQE_CHECK_ARG(n >= 0 && k >= 0 && k <= kBlockMax && d_t && (k == 0 || (h_vecs && h_coef)),
+                "bad block_axpy arguments (at most 64 vectors)");
+  if (k == 0 || n == 0) return FQEGPU_OK;
+  VecPtrs V;
+  Coefs c;
+  for (int i = 0; i < k; ++i) {
+    FQE_CHECK_ARG(h_vecs[i], "NULL vector");
+    V.p[i] = (const double2*)h_vecs[i];
+    c.c[i] = make_double2(h_coef[2 * i], h_coef[2 * i + 1]);
+  }
+  k_block_axpy<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, k, V, c, (double2*)d_t);
+  FQE_CUDA(cudaGetLastError());
   return FQEGPU_OK;
 }

@@ -57,6 +57,8 @@ _SIGNATURES = {
     "fqegpu_scale": [_L, _D, _D, _P, _P],
     "fqegpu_vdot": [_L, _P, _P, _P, _P],
     "fqegpu_norm2": [_L, _P, _P, _P],
+    "fqegpu_block_vdot": [_L, _I, _P, _P, _P, _P],
+    "fqegpu_block_axpy": [_L, _I, _P, _P, _P, _P],
     "fqegpu_taylor": [_P, _P, _D, _D, _D, _D, _I, _I,
                       ctypes.POINTER(_I), _P],
     "fqegpu_diagonal": [_P, _P, _P],

@@ -92,6 +92,33 @@ def _norm(x: torch.Tensor) -> float:
     return out.value
 
 
+def _ptrs(vs: List[torch.Tensor]):
+    return (ctypes.c_void_p * len(vs))(*[v.data_ptr() for v in vs])
+
+
+def _block_vdot(vs: List[torch.Tensor], t: torch.Tensor) -> numpy.ndarray:
+    """[<v_i | t>] for all i, one synchronisation."""
+    out = numpy.zeros(len(vs), dtype=numpy.complex128)
+    for k0 in range(0, len(vs), 64):
+        chunk = vs[k0:k0 + 64]
+        res = numpy.zeros(2 * len(chunk))
+        _lib.call("fqegpu_block_vdot", t.numel(), len(chunk), _ptrs(chunk),
+                  _ptr(t), res.ctypes.data_as(ctypes.c_void_p), _stream())
+        out[k0:k0 + len(chunk)] = res[0::2] + 1j * res[1::2]
+    return out
+
+
+def _block_axpy(coef, vs: List[torch.Tensor], t: torch.Tensor) -> None:
+    """t += sum_i coef[i] v_i, one pass over t."""
+    coef = numpy.asarray(coef, dtype=numpy.complex128)
+    for k0 in range(0, len(vs), 64):
+        chunk = vs[k0:k0 + 64]
+        c = numpy.ascontiguousarray(coef[k0:k0 + len(chunk)]).view(numpy.float64)
+        _lib.call("fqegpu_block_axpy", t.numel(), len(chunk),
+                  c.ctypes.data_as(ctypes.c_void_p), _ptrs(chunk), _ptr(t),
+                  _stream())
+
+
 def _scale(a: complex, x: torch.Tensor) -> None:
     a = complex(a)
     _lib.call("fqegpu_scale", x.numel(), a.real, a.imag, _ptr(x), _stream())
@@ -160,9 +187,9 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
     AV: List[torch.Tensor] = []
 
     def orthonormal_add(t: torch.Tensor) -> bool:
-        for _ in range(2):  # classical Gram-Schmidt, twice
-            for v in V:
-                _axpy(-_vdot(v, t), v, t)
+        for _ in range(2):  # block classical Gram-Schmidt, twice
+            if V:
+                _block_axpy(-_block_vdot(V, t), V, t)
         nrm = _norm(t)
         if nrm < 1.0e-10:
             return False
@@ -195,20 +222,18 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
         m = len(V)
         Tn = numpy.zeros((m, m), dtype=numpy.complex128)
         Tn[:T.shape[0], :T.shape[1]] = T
-        for i in range(m):
-            for j in range(m):
-                if i < T.shape[0] and j < T.shape[1]:
-                    continue
-                Tn[i, j] = _vdot(V[i], AV[j])
+        for j in range(T.shape[1], m):   # columns of the new vectors
+            Tn[:, j] = _block_vdot(V, AV[j])
+        for j in range(T.shape[1]):       # rows of the new vectors (Hermitian)
+            Tn[T.shape[0]:, j] = numpy.conj(Tn[j, T.shape[0]:])
         T = 0.5 * (Tn + Tn.conj().T)
         w, y = numpy.linalg.eigh(T)
         X, AX, R, res = [], [], [], []
         for j in range(block):
             x = torch.zeros_like(V[0])
             ax = torch.zeros_like(V[0])
-            for i in range(m):
-                _axpy(y[i, j], V[i], x)
-                _axpy(y[i, j], AV[i], ax)
+            _block_axpy(y[:, j], V, x)
+            _block_axpy(y[:, j], AV, ax)
             r = ax.clone()
             _axpy(-w[j], x, r)
             X.append(x)

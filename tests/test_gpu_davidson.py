@@ -117,3 +117,28 @@ def test_errors(gpu, golden):
         davidson.davidsonliu_fqe(ham, 1, [a, b], nele=4, sz=0, norb=6)
     with pytest.raises(ValueError):
         davidson.davidson(ham, 2, 2, nroots=226)
+
+
+def test_block_vector_ops(gpu):
+    # fqegpu_block_vdot / fqegpu_block_axpy against numpy, k up to 70
+    # (two chunks of at most 64 on the host side)
+    import torch
+    from fqe_gb300 import davidson
+    rng = numpy.random.default_rng(9)
+    n = 20011
+    for k in (1, 7, 64, 70):
+        vs_h = [rng.normal(size=n) + 1j * rng.normal(size=n) for _ in range(k)]
+        t_h = rng.normal(size=n) + 1j * rng.normal(size=n)
+        vs = [torch.from_numpy(v).cuda() for v in vs_h]
+        t = torch.from_numpy(t_h).cuda()
+        got = davidson._block_vdot(vs, t)
+        want = numpy.array([numpy.vdot(v, t_h) for v in vs_h])
+        numpy.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-10)
+        coef = rng.normal(size=k) + 1j * rng.normal(size=k)
+        davidson._block_axpy(coef, vs, t)
+        want_t = t_h + sum(c * v for c, v in zip(coef, vs_h))
+        numpy.testing.assert_allclose(t.cpu().numpy(), want_t, rtol=1e-13,
+                                      atol=1e-12)
+        # deterministic: the same reduction twice gives identical bits
+        assert numpy.array_equal(davidson._block_vdot(vs, t),
+                                 davidson._block_vdot(vs, t))
