@@ -192,6 +192,16 @@ int fqegpu_block_vdot(int64_t n, int k, const double *const *h_vecs,
 int fqegpu_block_axpy(int64_t n, int k, const double *h_coef,
                       const double *const *h_vecs, double *d_t, void *stream);
 
+/* ---- one-particle RDM -------------------------------------------------------
+ * h_rdm[i][j] = <bra| E_ij |ket>, E_ij = sum over spin of a+_i a_j, complex128
+ * [norb][norb] on the host: FqeData.rdm1(bradata) with ket = self and bra =
+ * bradata (fqe_data.py:1668-1724; the blocked dvec contraction of
+ * make_dvec_part, lib/fqe_data.c:604-639).  d_bra and d_ket are sector
+ * coefficient arrays of the graph's sector.  D is formed on the fly, never
+ * stored; deterministic; synchronises on `stream`. */
+int fqegpu_rdm1(fqegpu_graph g, const double *d_bra, const double *d_ket,
+                double *h_rdm, void *stream);
+
 /* ---- A10: Taylor propagator ------------------------------------------------
  * d_psi <- sum_k (-i t H)^k / k! d_psi until ||term|| < accuracy, at most
  * `expansion`-1 orders, then the e_0 phase exp(-i t e_0) (e0 passed in).

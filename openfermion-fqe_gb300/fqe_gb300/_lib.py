@@ -62,6 +62,7 @@ _SIGNATURES = {
     "fqegpu_taylor": [_P, _P, _D, _D, _D, _D, _I, _I,
                       ctypes.POINTER(_I), _P],
     "fqegpu_diagonal": [_P, _P, _P],
+    "fqegpu_rdm1": [_P, _P, _P, _P, _P],
     "fqegpu_precondition": [_L, _P, _P, _D, _D, _P, _P],
     "fqegpu_mlp_create": [ctypes.POINTER(_P)],
     "fqegpu_mlp_destroy": [_P],

@@ -305,6 +305,20 @@ class FqeData:
         return out
 
     # -- Davidson support -----------------------------------------------------
+    def rdm1(self, bradata: Optional["FqeData"] = None):
+        """fqe_data.py:1668-1724: (rdm1,) with rdm1[i][j] = <bra| E_ij |self>,
+        bra = bradata or self (spin-summed, complex128 [norb][norb])."""
+        bra = self if bradata is None else bradata
+        if (bra.nalpha(), bra.nbeta(), bra.norb()) != (
+                self.nalpha(), self.nbeta(), self.norb()):
+            raise ValueError("rdm1: bra and ket sectors differ")
+        norb = self.norb()
+        out = numpy.zeros((norb, norb), dtype=numpy.complex128)
+        _lib.call("fqegpu_rdm1", self._core.handle, _ptr(bra.coeff),
+                  _ptr(self.coeff), out.ctypes.data_as(ctypes.c_void_p),
+                  _stream())
+        return (out,)
+
     def diagonal_energies(self, h1e, h2e) -> torch.Tensor:
         """<I|H|I> for every determinant (Slater-Condon, one pass)."""
         ham = ham_for(self._core, h1e, h2e)

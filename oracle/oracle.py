@@ -15,6 +15,8 @@ reference keeps in Python:
 * ``evolve_diagonal_coulomb`` / ``apply_diagonal_coulomb``
                                   fqe_data.py:263-361 -> lib/fqe_data.c:455-602
 * ``make_dvec`` / ``make_coeff``  fqe_data.py:2209-2234, 2309-2334
+* ``rdm1``                        FqeData.rdm1 / _rdm1_blocked (fqe_data.py:1668-1724):
+                                  rdm1[i][j] = <bra|E_ij|ket> through make_dvec
 * ``diagonal_energies``           <I|H|I> for a restricted Hamiltonian, by
                                   applying H to unit vectors (small cases only)
 
@@ -321,3 +323,11 @@ def dense_hamiltonian(h1, h2, g: Graph):
         H[:, k] = apply_spatial12(e, h1, h2, g).ravel()
         e[a, b] = 0.0
     return H
+
+
+def rdm1(ket, g: Graph, bra=None):
+    """FqeData.rdm1(bradata) with ket = self (fqe_data.py:1668-1724):
+    rdm1[i][j] = <bra| E_ij |ket> = sum_I conj(bra_I) dvec_ket[i, j, I]."""
+    bra = ket if bra is None else bra
+    dvec = make_dvec(ket, g)  # [norb, norb, lena, lenb]
+    return numpy.tensordot(dvec, numpy.conj(bra), axes=((2, 3), (0, 1)))

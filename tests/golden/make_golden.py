@@ -217,8 +217,30 @@ def davidson_fixture():
          k4_e_ref_davidson=numpy.asarray(w_k))
 
 
+def rdm_fixture():
+    """FqeData.rdm1 of the reference (fqe_data.py:1668-1724), both branches of
+    its code-path switch, plus a transition RDM (bradata given)."""
+    out = {}
+    for norb, na, nb, seed in [(4, 2, 1, 0), (5, 2, 2, 1), (6, 3, 2, 2)]:
+        rng = numpy.random.default_rng(5000 + seed)
+        ket = FqeData(na, nb, norb)
+        bra = FqeData(na, nb, norb)
+        ket.coeff = synthetic.wavefunction_coeff(ket.lena(), ket.lenb(), rng)
+        bra.coeff = synthetic.wavefunction_coeff(bra.lena(), bra.lenb(), rng)
+        tag = f"{norb}_{na}_{nb}"
+        fqe.settings.use_accelerated_code = True
+        out[f"ket_{tag}"] = ket.coeff.copy()
+        out[f"bra_{tag}"] = bra.coeff.copy()
+        out[f"rdm1_{tag}"] = ket.rdm1()[0]
+        out[f"trdm1_{tag}"] = ket.rdm1(bra)[0]
+        fqe.settings.use_accelerated_code = False
+        out[f"rdm1py_{tag}"] = ket.rdm1()[0]
+        fqe.settings.use_accelerated_code = True
+    save("rdm", **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["graph", "apply", "dc", "taylor", "dvec",
-                             "davidson"]
+                             "davidson", "rdm"]
     for name in which:
         globals()[name + "_fixture"]()

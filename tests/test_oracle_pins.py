@@ -214,3 +214,18 @@ def test_davidson_known_answers_dense(golden, oracle):
     assert numpy.allclose(w4[:4], float(gd["k4_e_test"]), atol=1e-12)
     # the reference Davidson's eigenvalue-change rule stops above the exact root
     assert 1e-6 < gd["k4_e_ref_davidson"][0] - w4[0] < 1e-3
+
+
+def test_rdm1_matches_fixture(golden, oracle):
+    # FqeData.rdm1 of the reference, both code paths and a transition RDM
+    gd = golden("rdm")
+    for key in [k for k in gd if k.startswith("rdm1_")]:
+        tag = key[5:]
+        norb, na, nb = map(int, tag.split("_"))
+        g = oracle.graph(norb, na, nb)
+        r = oracle.rdm1(gd["ket_" + tag], g)
+        assert numpy.abs(r - gd["rdm1_" + tag]).max() < 1e-14
+        assert numpy.abs(r - gd["rdm1py_" + tag]).max() < 1e-14
+        t = oracle.rdm1(gd["ket_" + tag], g, gd["bra_" + tag])
+        assert numpy.abs(t - gd["trdm1_" + tag]).max() < 1e-14
+        assert abs(numpy.trace(r) - (na + nb)) < 1e-12  # normalised ket
