@@ -192,6 +192,25 @@ int fqegpu_block_vdot(int64_t n, int k, const double *const *h_vecs,
 int fqegpu_block_axpy(int64_t n, int k, const double *h_coef,
                       const double *const *h_vecs, double *d_t, void *stream);
 
+/* ---- batches of applies in one CUDA graph ----------------------------------
+ * No counterpart in the reference (Wavefunction._apply_array applies sectors
+ * one at a time, wavefunction.py:366-399).  Records n applies
+ *   d_sigmas[i] = alpha * (H_i d_psis[i]) + beta * d_psis[i]
+ * (hams may repeat; they run in order on one stream) into one CUDA graph after
+ * one uncaptured pass that allocates every workspace and tensor-core plan.
+ * fqegpu_batch_launch replays the batch with one graph launch (asynchronous);
+ * fqegpu_batch_check synchronises `stream` and reports a tensor-core timeout
+ * of the last launch.  Buffers are those given at creation. */
+typedef struct fqegpu_batch_s *fqegpu_batch;
+int fqegpu_batch_create(int n, const fqegpu_ham *hams,
+                        const double *const *d_psis, double *const *d_sigmas,
+                        double alpha_re, double alpha_im, double beta_re,
+                        double beta_im, int precision, void *stream,
+                        fqegpu_batch *out);
+int fqegpu_batch_launch(fqegpu_batch b, void *stream);
+int fqegpu_batch_check(fqegpu_batch b, void *stream);
+int fqegpu_batch_destroy(fqegpu_batch b);
+
 /* ---- one-particle RDM -------------------------------------------------------
  * h_rdm[i][j] = <bra| E_ij |ket>, E_ij = sum over spin of a+_i a_j, complex128
  * [norb][norb] on the host: FqeData.rdm1(bradata) with ket = self and bra =

@@ -54,6 +54,9 @@ struct fqegpu_ham_s {
   bool timing = false;
   std::vector<cudaEvent_t> events;
   int events_used = 0;
+  // Set while an apply is recorded into a CUDA graph: the tensor-core path
+  // then skips its end-of-apply error readback (fqegpu_batch_check reads it).
+  bool defer_check = false;
 };
 
 namespace fqegpu {
@@ -67,6 +70,8 @@ int apply_fp64(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
 int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
                 double2 beta, cudaStream_t st);
 void ozaki_destroy(fqegpu_ham h);
+// Error word of the tensor-core path's last apply (0 when none ran or OK).
+int ozaki_error_flag(fqegpu_ham h, int32_t* out);
 // Gather / scatter building blocks (apply.cu).
 int launch_gather(const fqegpu_graph_s* g, bool tri, int P, int64_t c0,
                   int64_t w, const double2* psi, double2* D, cudaStream_t st);

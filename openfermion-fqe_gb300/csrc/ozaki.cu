@@ -753,8 +753,16 @@ static int plan_create(fqegpu_ham h) {
     return FQEGPU_ERR_UNSUPPORTED;
   }
   pl->smem = fixed + (size_t)pl->ring * slot;
-  FQE_CUDA(cudaFuncSetAttribute(k_oz_mma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)pl->smem));
+  // the attribute belongs to the kernel, not to this plan: set the device
+  // maximum so plans of different sectors (different ring sizes) can coexist
+  FQE_CUDA(cudaFuncSetAttribute(k_oz_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+  return FQEGPU_OK;
+}
+
+int ozaki_error_flag(fqegpu_ham h, int32_t* out) {
+  *out = 0;
+  if (!h->oz) return FQEGPU_OK;
+  FQE_CUDA(cudaMemcpy(out, h->oz->d_misc + 1, sizeof(int32_t), cudaMemcpyDeviceToHost));
   return FQEGPU_OK;
 }
 
@@ -831,6 +839,7 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
                                    zmul_host(alpha, h->phase), beta, sigma);
   FQE_CUDA(cudaGetLastError());
   FQE_TRY(stage_mark(h, 0, 3, st));
+  if (h->defer_check) return FQEGPU_OK;  // recorded into a graph
   int32_t errv = 0;
   FQE_CUDA(cudaMemcpyAsync(&errv, pl->d_misc + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   FQE_CUDA(cudaStreamSynchronize(st));

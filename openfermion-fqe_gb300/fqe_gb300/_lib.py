@@ -63,6 +63,11 @@ _SIGNATURES = {
                       ctypes.POINTER(_I), _P],
     "fqegpu_diagonal": [_P, _P, _P],
     "fqegpu_rdm1": [_P, _P, _P, _P, _P],
+    "fqegpu_batch_create": [_I, _P, _P, _P, _D, _D, _D, _D, _I, _P,
+                            ctypes.POINTER(_P)],
+    "fqegpu_batch_launch": [_P, _P],
+    "fqegpu_batch_check": [_P, _P],
+    "fqegpu_batch_destroy": [_P],
     "fqegpu_precondition": [_L, _P, _P, _D, _D, _P, _P],
     "fqegpu_mlp_create": [ctypes.POINTER(_P)],
     "fqegpu_mlp_destroy": [_P],

@@ -103,3 +103,17 @@ def test_ozaki_deterministic(ozaki):
     a = _apply(ozaki, 10, 5, 4, h1, h2, psi)
     b = _apply(ozaki, 10, 5, 4, h1, h2, psi)
     assert numpy.array_equal(a, b)
+
+
+def test_plans_of_different_sizes_coexist(gpu, ozaki):
+    # a large sector's plan first, then a small one, then the large one again:
+    # the contraction kernel's shared-memory limit must fit every plan
+    from fqe_gb300 import synthetic
+    outs = []
+    # shared memory per plan: norb 12 ~224 KB, norb 8 ~215 KB
+    for norb, na, nb in [(12, 6, 6), (8, 4, 4), (12, 6, 6)]:
+        h1, h2, psi = synthetic.sector(norb, na, nb, 2 * norb, seed=norb)
+        d = gpu.FqeData(na, nb, norb)
+        d.set_wfn(strategy="from_data", raw_data=psi)
+        outs.append(d.apply((h1, h2)).coeff.cpu().numpy())
+    assert numpy.array_equal(outs[0], outs[2])
