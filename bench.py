@@ -126,6 +126,24 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """Largest per-rank timing over the job (the job is as slow as its slowest
+    replica); the identity for one rank."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(n_per_rank: int, world: int, seconds: float) -> float:
+    """Whole-job determinant updates per second: every replica applies its own
+    full sector (weak scaling)."""
+    return world * n_per_rank / seconds
+
+
 def make_inputs():
     from fqe_gb300 import synthetic
     return synthetic.sector(NORB, NALPHA, NBETA, NCHOL, SEED)
@@ -248,12 +266,8 @@ def run_gpu(args):
     _lib.call("fqegpu_ham_set_timing", ham.handle, 0)
     clocks = clk.summary()
 
-    t_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = world * n / (t_max / 1e3)
+    t_max = max_over_ranks(ms, world)
+    value = job_value(n, world, t_max / 1e3)
 
     # e2e: host buffers through the C ABI (pinned)
     psi_pin = torch.from_numpy(psi_h).pin_memory()
@@ -270,11 +284,7 @@ def run_gpu(args):
     for _ in range(args.steps):
         step_e2e()
     barrier()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world)
     # correctness guard on the e2e output (cheap: norm of sigma vs device run)
     e2e_ok = bool(numpy.isfinite(out_pin.numpy()).all())
 
@@ -363,7 +373,7 @@ def run_gpu(args):
                    "l2": "inputs larger than L2 (psi 188 MB; D and G blocks "
                          f"{2 * 16 * P * n / 1e9:.1f} GB)",
                    "parallelism": f"replicas x{world}"},
-        "e2e": {"value": world * n / e2e_s, "unit": UNIT,
+        "e2e": {"value": job_value(n, world, e2e_s), "unit": UNIT,
                 "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n,
                 "finite": e2e_ok},
         "gpu_launches": launches_per_apply * args.steps,
