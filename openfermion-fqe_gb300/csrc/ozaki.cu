@@ -59,6 +59,7 @@ constexpr int kM = 128;        // MMA M (pairs, padded)
 constexpr int kN = 64;         // real columns of one slice tile
 constexpr int kNM = 128;       // MMA N: two slice tiles
 constexpr int kDets = 32;      // determinants per slice tile
+constexpr int kSuperTiles = 32;  // tiles per column super-block (1024 columns)
 constexpr int kChunkK = 16;    // K columns per streamed slice chunk (one MMA k-step)
 constexpr int kChunkElems = kN * kChunkK;  // 1024 BF16 = 2 KB
 constexpr int kPairChunkElems = 2 * kChunkElems;  // a K chunk of both tiles of a pair: 4 KB
@@ -110,11 +111,18 @@ struct OzArgs {
   int32_t* err;
 };
 
-// Tile t -> (alpha row, first beta column): row-major, 32 determinants.
+// Tile t -> (alpha row, first beta column).  Tiles are visited in column
+// super-blocks of kSuperTiles tiles (1024 determinants of a row), alpha rows
+// within a super-block: the 16-byte psi segments the alpha-source gathers read
+// (one 1024-column slice of every row, 16 KB each) then stay L2-resident.
 __device__ __forceinline__ void tile_coords(const OzArgs& A, int64_t t, int64_t& ia,
                                             int64_t& ib0) {
-  ia = t / A.nb;
-  ib0 = (t - ia * A.nb) * kDets;
+  const int64_t per_super = A.lena * kSuperTiles;
+  const int64_t sb = t / per_super;
+  const int64_t r = t - sb * per_super;
+  const int64_t w = min((int64_t)kSuperTiles, (int64_t)A.nb - sb * kSuperTiles);
+  ia = r / w;
+  ib0 = (sb * kSuperTiles + (r - ia * w)) * kDets;
 }
 
 // Bounded wait that also gives up when another role has aborted.
@@ -372,8 +380,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  // each CTA owns a contiguous run of tile pairs (consecutive tiles share an
-  // alpha row, so the G rows it writes are contiguous too)
+  // each CTA owns a contiguous run of tile pairs (in the super-block order of
+  // tile_coords)
   const int64_t t_begin = npairs * blockIdx.x / gridDim.x;
   const int64_t t_end = npairs * (blockIdx.x + 1) / gridDim.x;
 
