@@ -69,7 +69,6 @@ constexpr int kEpiWarps = 16;  // four per TMEM lane quarter, 32 columns each
 constexpr int kMmaWarp = 16;
 constexpr int kLoadWarp = 17;
 constexpr int kThreads = 18 * 32;
-constexpr int kSliceThreads = 512;  // one CTA of k_oz_slice = one tile
 constexpr int kAccs = 4;           // levels 2, 3, 4 and 5..7
 constexpr uint32_t kTmemCols = kAccs * kNM;  // 512: one accumulator set
 constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
@@ -78,16 +77,18 @@ constexpr int kExpZero = -2000;
 
 struct OzakiPlan {
   int P = 0, KP = 0;
-  __nv_bfloat16* d_vslices = nullptr;  // [5][128 * KP] canonical K-major
-  int32_t* d_vexp = nullptr;           // [128]
+  int npass = 1, NP = 0;               // output pairs in passes of NP rows
+  int64_t wb = 0;                      // beta columns per block (multiple of 32)
+  __nv_bfloat16* d_vslices = nullptr;  // [npass][5][NP * KP] canonical K-major
+  int32_t* d_vexp = nullptr;           // [npass * NP] row exponents
   longlong2* d_psix = nullptr;         // [N]
   int32_t* d_rowexp = nullptr;         // [lena]
   int32_t* d_misc = nullptr;           // [0] = global exponent, [1] = error
-  float4* d_G = nullptr;               // [P][N]
+  float4* d_G = nullptr;               // [P][lena][wb]
   uchar2* d_bexp = nullptr;            // [N]
   int32_t* d_tabTA = nullptr;          // [lena][KP] target tables, pair index fastest
   int32_t* d_tabTB = nullptr;          // [lenb][KP]
-  __nv_bfloat16* d_dslices = nullptr;  // [ntiles][5][64 * KP] smem images
+  __nv_bfloat16* d_dslices = nullptr;  // [tiles of a block][5][64 * KP] smem images
   int ring = 0;
   int nsm = 0;
   size_t smem = 0;
@@ -95,8 +96,10 @@ struct OzakiPlan {
 
 struct OzArgs {
   int P, KP, ring;
-  int64_t lena, lenb, ntiles;
-  int nb;  // column blocks per row
+  int NP, p0;        // this pass: N = NP output pairs starting at p0
+  int64_t lena, lenb, ntiles;  // ntiles: tiles of this beta-column block
+  int nb;            // tiles per alpha row in this block
+  int64_t c0, gld;   // first column of the block; row length of G (block width)
   const int32_t* tabA;
   const int32_t* tabB;
   const int32_t* tabTA;  // [lena][KP]: the 8 pairs of an octet are 32 contiguous bytes
@@ -122,7 +125,7 @@ __device__ __forceinline__ void tile_coords(const OzArgs& A, int64_t t, int64_t&
   const int64_t r = t - sb * per_super;
   const int64_t w = min((int64_t)kSuperTiles, (int64_t)A.nb - sb * kSuperTiles);
   ia = r / w;
-  ib0 = (sb * kSuperTiles + (r - ia * w)) * kDets;
+  ib0 = A.c0 + (sb * kSuperTiles + (r - ia * w)) * kDets;
 }
 
 // Bounded wait that also gives up when another role has aborted.
@@ -228,8 +231,9 @@ __device__ __forceinline__ uint32_t bf16_bytes_pair(uint32_t w, int k, uint32_t 
 // (a warp stores 1 KB contiguous per instruction pair) and the exact exponent
 // of every real column (shuffle maximum inside a warp, shared memory across
 // the two warps of a determinant group).
-__global__ void __launch_bounds__(kSliceThreads, 2) k_oz_slice(OzArgs A) {
-  __shared__ int red[16][4];
+template <int H>  // H groups of eight octets: KP <= 64 H
+__global__ void __launch_bounds__(256 * H, H == 2 ? 2 : 1) k_oz_slice(OzArgs A) {
+  __shared__ int red[8 * H][4];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int grp = w & 7, half = w >> 3;
   const int64_t t = blockIdx.x;
@@ -276,9 +280,12 @@ __global__ void __launch_bounds__(kSliceThreads, 2) k_oz_slice(OzArgs A) {
   }
   if (lane < 4) red[w][lane] = blr | (bli << 8);
   __syncthreads();
-  const int other = red[w ^ 8][lane & 3];
-  blr = max(blr, other & 0xFF);
-  bli = max(bli, other >> 8);
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    const int other = red[grp + 8 * h][lane & 3];
+    blr = max(blr, other & 0xFF);
+    bli = max(bli, other >> 8);
+  }
   if (half == 0 && lane < 4 && valid)
     A.bexp[ia * lenb32 + ib] = make_uchar2((unsigned char)blr, (unsigned char)bli);
   uint32_t pk[2][2 * kSlices];
@@ -337,7 +344,8 @@ __global__ void __launch_bounds__(kSliceThreads, 2) k_oz_slice(OzArgs A) {
 __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int KP = A.KP, R = A.ring;
-  const uint32_t v_elems = (uint32_t)KP * KP;
+  const int NP = A.NP;
+  const uint32_t v_elems = (uint32_t)NP * KP;
   const uint32_t slot_elems = (uint32_t)(kGroupK * kPairChunkElems);
   const uint32_t pchunk_bytes = (uint32_t)kPairChunkElems * 2u;
   const int nch = KP / kChunkK;                       // chunks per slice
@@ -360,7 +368,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
     int4* dst = reinterpret_cast<int4*>(sV);
     const int n16 = (int)(kSlices * v_elems * 2 / 16);
     for (int i = tid; i < n16; i += blockDim.x) dst[i] = src[i];
-    for (int i = tid; i < kM; i += blockDim.x) sVexp[i] = A.vexp[i];
+    for (int i = tid; i < NP; i += blockDim.x) sVexp[i] = A.vexp[i];
   }
   if (tid == 0) {
     for (int i = 0; i < R; ++i) {
@@ -417,7 +425,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
     }
   } else if (warp == kMmaWarp) {
     if (lane == 0) {
-      const uint32_t idesc = tc::make_idesc_bf16(kM, (uint32_t)KP);
+      const uint32_t idesc = tc::make_idesc_bf16(kM, (uint32_t)NP);
       const uint32_t sbo = (uint32_t)KP * 16u;          // V: full-K rows
       const uint32_t sbo_c = (uint32_t)kChunkK * 16u;   // D chunk: 16-column rows
       // B = V slice descriptors of k-step 0; k-step ks adds 256 bytes = 16 units
@@ -460,7 +468,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
                   if (a <= amax) {
                     const int lvl = a + b;
                     const int ai = lvl <= 4 ? lvl - 2 : 3;
-                    const uint32_t acc = tmem + (uint32_t)(ai * KP);
+                    const uint32_t acc = tmem + (uint32_t)(ai * NP);
                     // A (D chunk) advances one 4 KB pair chunk = 256 units per
                     // k-step; B (V slice a) advances 256 bytes = 16 units
                     tc::mma_bf16(acc, dd + (uint64_t)(256 * c),
@@ -491,7 +499,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
     const int half = row >> 6;                // slice tile of the pair
     const int det = (row & 63) >> 1;          // determinant in that tile
     const int part = row & 1;                 // 0 real, 1 imaginary
-    const int cw = KP / 4;                    // pairs per column group
+    const int cw = NP / 4;                    // pairs per column group
     const int pbeg = cg * cw;
     const int g0 = A.misc[0];
     int64_t it = 0;
@@ -516,23 +524,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       tc::fence_after_sync();
       const uint32_t base = tmem + ((uint32_t)(32 * quarter) << 16);
       // this lane's half of G[p][det]: (hi, lo) of the real or imaginary part
-      float2* gcol = reinterpret_cast<float2*>(A.G + ia * A.lenb + ib) + part;
-      const int64_t pstride = A.lena * A.lenb * 2;  // float2 elements per pair row
+      float2* gcol = reinterpret_cast<float2*>(A.G + ia * A.gld + (ib - A.c0)) + part;
+      const int64_t pstride = A.lena * A.gld * 2;  // float2 elements per pair row
       for (int c0 = 0; c0 < cw; c0 += 4) {
         const int pc = pbeg + c0;
         uint32_t ra[4], rb[4], rc[4], rd[4];
         tc::tmem_ld4_nowait(base + (uint32_t)pc, ra);
-        tc::tmem_ld4_nowait(base + (uint32_t)(KP + pc), rb);
-        tc::tmem_ld4_nowait(base + (uint32_t)(2 * KP + pc), rc);
-        tc::tmem_ld4_nowait(base + (uint32_t)(3 * KP + pc), rd);
+        tc::tmem_ld4_nowait(base + (uint32_t)(NP + pc), rb);
+        tc::tmem_ld4_nowait(base + (uint32_t)(2 * NP + pc), rc);
+        tc::tmem_ld4_nowait(base + (uint32_t)(3 * NP + pc), rd);
         tc::tmem_wait_ld();
         if (!live) continue;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          const int p = pc + k;
+          const int p = A.p0 + pc + k;
           if (p >= A.P) break;
           // column exponent: |D| < 2^(bits - 62 + g0); row exponent of V
-          const int sc = sVexp[p] + bits - 62 + g0;
+          const int sc = sVexp[pc + k] + bits - 62 + g0;
           const float x = __uint_as_float(ra[k]), y = __uint_as_float(rb[k]);
           // exact two-sum of levels 2 and 3, then levels 4 and 5..7
           const float h = x + y;
@@ -638,38 +646,54 @@ __device__ __forceinline__ double2 zmul2(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// sigma[I] (init: beta psi[I] +, else sigma[I] +) alpha * the contributions of
+// the beta-column block [c0, c0 + w) held in G ([P][lena][w]): the alpha part
+// of targets in the block, the beta part of every target whose source column
+// lies in the block (G rows have gld entries).  One block covering all
+// columns is the whole apply.
 __global__ void __launch_bounds__(256) k_oz_scatter(
-    int P, int64_t lena, int64_t lenb, const int32_t* __restrict__ tabA,
+    int P, int64_t lena, int64_t lenb, int64_t c0, int64_t w, int64_t gld,
+    const int32_t* __restrict__ tabA,
     const int32_t* __restrict__ tabB, const float4* __restrict__ G,
-    const double2* __restrict__ psi, double2 alpha, double2 beta,
+    const double2* __restrict__ psi, double2 alpha, double2 beta, int init,
     double2* __restrict__ sigma) {
   const int64_t a = blockIdx.y;
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= lenb) return;
+  const bool inblk = b >= c0 && b < c0 + w;
   float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
   for (int p = 0; p < P; ++p) {
     const int32_t ca = tabA[(int64_t)p * lena + a];
-    if (ca) {
-      float4 g = G[((int64_t)p * lena + (abs(ca) - 1)) * lenb + b];
+    if (ca && inblk) {
+      float4 g = G[((int64_t)p * lena + (abs(ca) - 1)) * gld + (b - c0)];
       if (ca < 0) g = make_float4(-g.x, -g.y, -g.z, -g.w);
       df_add(rh, rl, g.x, g.y);
       df_add(ih, il, g.z, g.w);
     }
     const int32_t cb = tabB[(int64_t)p * lenb + b];
     if (cb) {
-      float4 g = G[((int64_t)p * lena + a) * lenb + (abs(cb) - 1)];
-      if (cb < 0) g = make_float4(-g.x, -g.y, -g.z, -g.w);
-      df_add(rh, rl, g.x, g.y);
-      df_add(ih, il, g.z, g.w);
+      const int64_t J = abs(cb) - 1;
+      if (J >= c0 && J < c0 + w) {
+        float4 g = G[((int64_t)p * lena + a) * gld + (J - c0)];
+        if (cb < 0) g = make_float4(-g.x, -g.y, -g.z, -g.w);
+        df_add(rh, rl, g.x, g.y);
+        df_add(ih, il, g.z, g.w);
+      }
     }
   }
   const int64_t I = a * lenb + b;
   const double2 acc = make_double2((double)rh + (double)rl, (double)ih + (double)il);
   double2 out = zmul2(alpha, acc);
-  if (beta.x != 0.0 || beta.y != 0.0) {
-    const double2 t = zmul2(beta, psi[I]);
-    out.x += t.x;
-    out.y += t.y;
+  if (init) {
+    if (beta.x != 0.0 || beta.y != 0.0) {
+      const double2 t = zmul2(beta, psi[I]);
+      out.x += t.x;
+      out.y += t.y;
+    }
+  } else {
+    const double2 s0 = sigma[I];
+    out.x += s0.x;
+    out.y += s0.y;
   }
   sigma[I] = out;
 }
@@ -685,27 +709,54 @@ __global__ void k_oz_transpose_tab(int P, int KP, int64_t len, const int32_t* __
 }
 
 // ---- host ---------------------------------------------------------------------
+// Shape of the tensor-core form for P pairs: K = KP (pairs rounded up to 16),
+// output pairs in npass passes of NP rows (four level accumulators of NP TMEM
+// columns, NP <= 128; five NP x KP V slices in shared memory beside a ring of
+// at least two slots).  False when the sector does not fit (FP64 kernels).
+static bool oz_shape(int P, int smax, int& KP, int& npass, int& NP, size_t& fixed) {
+  KP = (P + 15) / 16 * 16;
+  if (KP > 192) return false;  // the slicer covers 24 octets of pairs
+  npass = KP <= kM ? 1 : 2;
+  NP = ((P + npass - 1) / npass + 15) / 16 * 16;
+  if (NP > kM) return false;
+  fixed = sizeof(__nv_bfloat16) * (size_t)kSlices * NP * KP +
+          sizeof(uint64_t) * (2 * kMaxRing + 3) + 16 + sizeof(int) * kM;
+  const size_t slot = sizeof(__nv_bfloat16) * (size_t)kGroupK * kPairChunkElems;
+  return fixed + 2 * slot <= (size_t)smax;
+}
+
 static int plan_create(fqegpu_ham h) {
+  int dev = 0, smax = 0;
+  FQE_CUDA(cudaGetDevice(&dev));
+  FQE_CUDA(cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const int P = h->P;
+  int KP = 0, npass = 0, NP = 0;
+  size_t fixed = 0;
+  if (!oz_shape(P, smax, KP, npass, NP, fixed)) {
+    set_error("pair count %d does not fit the tensor-core contraction", P);
+    return FQEGPU_ERR_UNSUPPORTED;
+  }
   auto* pl = new (std::nothrow) OzakiPlan();
   if (!pl) {
     set_error("host allocation failed");
     return FQEGPU_ERR_NOMEM;
   }
   h->oz = pl;
-  const int P = h->P;
-  const int KP = (P + 15) / 16 * 16;
   pl->P = P;
   pl->KP = KP;
-  const size_t vel = (size_t)KP * KP;  // V slice: KP rows (pairs) x KP
-  std::vector<__nv_bfloat16> sl(kSlices * vel, __float2bfloat16(0.0f));
-  std::vector<int32_t> vexp(kM, 0);
+  pl->npass = npass;
+  pl->NP = NP;
+  const size_t vel = (size_t)NP * KP;  // V slice of one pass: NP rows (pairs) x KP
+  std::vector<__nv_bfloat16> sl((size_t)npass * kSlices * vel, __float2bfloat16(0.0f));
+  std::vector<int32_t> vexp((size_t)npass * NP, 0);
   for (int p = 0; p < P; ++p) {
+    const int pass = p / NP, r = p - pass * NP;
     double mx = 0.0;
     for (int q = 0; q < P; ++q) mx = std::max(mx, std::fabs(h->vpair[(size_t)p * P + q]));
     if (mx == 0.0) continue;
     int e;
     std::frexp(mx, &e);  // mx < 2^e
-    vexp[p] = e;
+    vexp[(size_t)pass * NP + r] = e;
     for (int q = 0; q < P; ++q) {
       const double v = h->vpair[(size_t)p * P + q];
       const double y = std::floor(std::ldexp(std::fabs(v), 40 - e) + 0.5);
@@ -713,20 +764,32 @@ static int plan_create(fqegpu_ham h) {
       for (int k = 1; k <= kSlices; ++k) {
         const uint32_t byte = (uint32_t)((m >> (40 - 8 * k)) & 0xFFu);
         const float f = std::ldexp((float)byte, -8 * k) * (v < 0 ? -1.0f : 1.0f);
-        sl[(size_t)(k - 1) * vel + tc::kmajor_offset(p, q, KP)] = __float2bfloat16(f);
+        sl[((size_t)pass * kSlices + (k - 1)) * vel + tc::kmajor_offset(r, q, KP)] =
+            __float2bfloat16(f);
       }
     }
   }
   FQE_CUDA(cudaMalloc(&pl->d_vslices, sizeof(__nv_bfloat16) * sl.size()));
   FQE_CUDA(cudaMemcpy(pl->d_vslices, sl.data(), sizeof(__nv_bfloat16) * sl.size(),
                       cudaMemcpyHostToDevice));
-  FQE_CUDA(cudaMalloc(&pl->d_vexp, sizeof(int32_t) * kM));
-  FQE_CUDA(cudaMemcpy(pl->d_vexp, vexp.data(), sizeof(int32_t) * kM, cudaMemcpyHostToDevice));
+  FQE_CUDA(cudaMalloc(&pl->d_vexp, sizeof(int32_t) * vexp.size()));
+  FQE_CUDA(cudaMemcpy(pl->d_vexp, vexp.data(), sizeof(int32_t) * vexp.size(),
+                      cudaMemcpyHostToDevice));
   const int64_t lena = h->g->a.len, lenb = h->g->b.len, N = lena * lenb;
+  // beta-column blocks: slice images (20 KP bytes) and G (16 P bytes) per
+  // determinant of a block within the handle's scratch budget
+  const int64_t per_col = (int64_t)(20 * KP + 16 * P) * lena;
+  int64_t wb = h->scratch_limit / std::max<int64_t>(per_col, 1);
+  if (wb >= lenb) {
+    wb = lenb;  // one block: G is [P][lena][lenb]
+  } else {
+    wb = std::max<int64_t>(kDets, wb / kDets * kDets);
+  }
+  pl->wb = wb;
   FQE_CUDA(cudaMalloc(&pl->d_psix, sizeof(longlong2) * N));
   FQE_CUDA(cudaMalloc(&pl->d_rowexp, sizeof(int32_t) * lena));
   FQE_CUDA(cudaMalloc(&pl->d_misc, sizeof(int32_t) * 4));
-  FQE_CUDA(cudaMalloc(&pl->d_G, sizeof(float4) * (size_t)P * N));
+  FQE_CUDA(cudaMalloc(&pl->d_G, sizeof(float4) * (size_t)P * lena * wb));
   FQE_CUDA(cudaMalloc(&pl->d_bexp, sizeof(uchar2) * N));
   {
     const bool tri = h->compressed;
@@ -741,25 +804,15 @@ static int plan_create(fqegpu_ham h) {
     FQE_CUDA(cudaGetLastError());
     FQE_CUDA(cudaDeviceSynchronize());
   }
-  const int64_t ntiles = lena * ((lenb + kDets - 1) / kDets);
+  const int64_t ntiles = lena * ((wb + kDets - 1) / kDets);  // tiles of the widest block
   const int64_t npairs = (ntiles + 1) / 2;
   const size_t dsl = sizeof(__nv_bfloat16) * (size_t)npairs * 2 * kSlices * kN * KP;
   FQE_CUDA(cudaMalloc(&pl->d_dslices, dsl));
-  FQE_CUDA(cudaMemset(pl->d_dslices, 0, dsl));  // the unpaired last tile reads zeros
-  int dev = 0;
-  FQE_CUDA(cudaGetDevice(&dev));
+  FQE_CUDA(cudaMemset(pl->d_dslices, 0, dsl));  // an unpaired last tile reads zeros
   FQE_CUDA(cudaDeviceGetAttribute(&pl->nsm, cudaDevAttrMultiProcessorCount, dev));
   // as many slice slots as shared memory holds after the V slices
-  int smax = 0;
-  FQE_CUDA(cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  const size_t fixed = sizeof(__nv_bfloat16) * (size_t)kSlices * vel +
-                       sizeof(uint64_t) * (2 * kMaxRing + 3) + 16 + sizeof(int) * kM;
   const size_t slot = sizeof(__nv_bfloat16) * (size_t)kGroupK * kPairChunkElems;
   pl->ring = (int)std::min<size_t>(kMaxRing, ((size_t)smax - fixed) / slot);
-  if (pl->ring < 2) {
-    set_error("shared memory too small for the tensor-core contraction");
-    return FQEGPU_ERR_UNSUPPORTED;
-  }
   pl->smem = fixed + (size_t)pl->ring * slot;
   // the attribute belongs to the kernel, not to this plan: set the device
   // maximum so plans of different sectors (different ring sizes) can coexist
@@ -793,9 +846,9 @@ void ozaki_destroy(fqegpu_ham h) {
 
 int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
                 double2 beta, cudaStream_t st) {
-  // The split needs a real pair matrix that fits one 128-row MMA tile; other
-  // operators run the FP64 kernels on the GPU.
-  if (h->zero || h->onebody || !h->real || h->P > kM)
+  // The split needs a real pair matrix whose shape fits the kernels (P <= 192,
+  // shared memory); other operators run the FP64 kernels on the GPU.
+  if (h->zero || h->onebody || !h->real || h->P > 192)
     return apply_fp64(h, psi, sigma, alpha, beta, st);
   const fqegpu_graph_s* g = h->g;
   const int64_t lena = g->a.len, lenb = g->b.len, N = lena * lenb;
@@ -804,7 +857,11 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
               (long long)lena);
     return FQEGPU_ERR_UNSUPPORTED;
   }
-  if (!h->oz) FQE_TRY(plan_create(h));
+  if (!h->oz) {
+    const int s = plan_create(h);
+    if (s == FQEGPU_ERR_UNSUPPORTED && !h->oz) return apply_fp64(h, psi, sigma, alpha, beta, st);
+    FQE_TRY(s);
+  }
   OzakiPlan* pl = h->oz;
   const bool tri = h->compressed;
   const int32_t* tabA = tri ? g->a.tab_tri : g->a.tab_full;
@@ -819,34 +876,50 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   A.P = pl->P;
   A.KP = pl->KP;
   A.ring = pl->ring;
+  A.NP = pl->NP;
   A.lena = lena;
   A.lenb = lenb;
-  A.nb = (int)((lenb + kDets - 1) / kDets);
-  A.ntiles = lena * (int64_t)A.nb;
+  A.gld = pl->wb;
   A.tabA = tabA;
   A.tabB = tabB;
   A.psix = pl->d_psix;
   A.misc = pl->d_misc;
-  A.vslices = pl->d_vslices;
-  A.vexp = pl->d_vexp;
   A.G = pl->d_G;
   A.bexp = pl->d_bexp;
   A.tabTA = pl->d_tabTA;
   A.tabTB = pl->d_tabTB;
   A.dslices = pl->d_dslices;
   A.err = pl->d_misc + 1;
-  k_oz_slice<<<(unsigned)A.ntiles, kSliceThreads, 0, st>>>(A);
-  FQE_CUDA(cudaGetLastError());
-  FQE_TRY(stage_mark(h, 0, 1, st));
-  const int grid = (int)std::min<int64_t>(pl->nsm, (A.ntiles + 1) / 2);
-  k_oz_mma<<<grid, kThreads, pl->smem, st>>>(A);
-  FQE_CUDA(cudaGetLastError());
-  FQE_TRY(stage_mark(h, 0, 2, st));
-  dim3 sg((unsigned)((lenb + 255) / 256), (unsigned)lena);
-  k_oz_scatter<<<sg, 256, 0, st>>>(pl->P, lena, lenb, tabA, tabB, pl->d_G, psi,
-                                   zmul_host(alpha, h->phase), beta, sigma);
-  FQE_CUDA(cudaGetLastError());
-  FQE_TRY(stage_mark(h, 0, 3, st));
+  const size_t vel = (size_t)pl->NP * pl->KP;
+  const double2 al = zmul_host(alpha, h->phase);
+  int blk = 0;
+  for (int64_t c0 = 0; c0 < lenb; c0 += pl->wb, ++blk) {
+    const int64_t w = std::min<int64_t>(pl->wb, lenb - c0);
+    A.c0 = c0;
+    A.nb = (int)((w + kDets - 1) / kDets);
+    A.ntiles = lena * (int64_t)A.nb;
+    if (blk > 0) FQE_TRY(stage_mark(h, blk, 0, st));
+    if (A.KP <= 128)
+      k_oz_slice<2><<<(unsigned)A.ntiles, 512, 0, st>>>(A);
+    else
+      k_oz_slice<3><<<(unsigned)A.ntiles, 768, 0, st>>>(A);
+    FQE_CUDA(cudaGetLastError());
+    FQE_TRY(stage_mark(h, blk, 1, st));
+    const int grid = (int)std::min<int64_t>(pl->nsm, (A.ntiles + 1) / 2);
+    for (int pass = 0; pass < pl->npass; ++pass) {
+      A.p0 = pass * pl->NP;
+      A.vslices = pl->d_vslices + (size_t)pass * kSlices * vel;
+      A.vexp = pl->d_vexp + (size_t)pass * pl->NP;
+      k_oz_mma<<<grid, kThreads, pl->smem, st>>>(A);
+      FQE_CUDA(cudaGetLastError());
+    }
+    FQE_TRY(stage_mark(h, blk, 2, st));
+    dim3 sg((unsigned)((lenb + 255) / 256), (unsigned)lena);
+    k_oz_scatter<<<sg, 256, 0, st>>>(pl->P, lena, lenb, c0, w, pl->wb, tabA, tabB, pl->d_G,
+                                     psi, al, beta, blk == 0 ? 1 : 0, sigma);
+    FQE_CUDA(cudaGetLastError());
+    FQE_TRY(stage_mark(h, blk, 3, st));
+  }
   if (h->defer_check) return FQEGPU_OK;  // recorded into a graph
   int32_t errv = 0;
   FQE_CUDA(cudaMemcpyAsync(&errv, pl->d_misc + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, st));

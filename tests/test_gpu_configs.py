@@ -4,10 +4,9 @@ finishes in seconds, plus size-independent properties at full size):
 * uneven sectors over norb {8, 10, 12}, each with its own seeded integrals
   (seed = index), one apply and a Taylor evolution t = 0.1 to 1e-10, FP64 and
   tensor-core paths against the oracle;
-* norb 16: a (3, 3) sector (P = 136 compressed pairs, beyond the tensor-core
-  tile, so both precisions run the FP64 kernels) against the oracle, a short
-  Taylor evolution, and the full (8, 8) sector through Hermiticity of the
-  apply.
+* norb 16: a (3, 3) sector (P = 136 compressed pairs: the tensor-core form
+  runs two passes of output pairs) against the oracle, a short Taylor
+  evolution, and the full (8, 8) sector through Hermiticity of the apply.
 """
 
 import math
@@ -76,7 +75,9 @@ def test_norb16_sector(gpu, oracle, precision):
         w = _wfn(gpu, norb, na, nb, psi)
         out = w.apply(ham).get_coeff((na + nb, na - nb)).cpu().numpy()
         want = oracle.apply_restricted(psi, (h1, h2), 0.0, g)
-        assert _rel(out, want) < TOL_FP64  # P = 136: FP64 kernels either way
+        # P = 136: the tensor-core form runs in two passes of 80 output pairs
+        tol = TOL_FP64 if precision == "fp64" else TOL_OZ
+        assert _rel(out, want) < tol
         # two Taylor steps of dt = 0.05: norm and fidelity against the oracle
         cur, ref = w, psi
         for _ in range(2):
@@ -84,8 +85,8 @@ def test_norb16_sector(gpu, oracle, precision):
             ref, _ = oracle.taylor_evolve(ref, (h1, h2), 0.0, 0.05, g,
                                           accuracy=1e-12)
             got = cur.get_coeff((na + nb, na - nb)).cpu().numpy()
-            assert abs(numpy.linalg.norm(got) - 1.0) < 1e-11
-            assert abs(abs(numpy.vdot(ref.ravel(), got.ravel())) - 1.0) < 1e-11
+            assert abs(numpy.linalg.norm(got) - 1.0) < 10 * tol
+            assert abs(abs(numpy.vdot(ref.ravel(), got.ravel())) - 1.0) < 10 * tol
     finally:
         settings.precision = old
 

@@ -117,3 +117,24 @@ def test_plans_of_different_sizes_coexist(gpu, ozaki):
         d.set_wfn(strategy="from_data", raw_data=psi)
         outs.append(d.apply((h1, h2)).coeff.cpu().numpy())
     assert numpy.array_equal(outs[0], outs[2])
+
+
+@pytest.mark.parametrize("norb,na,nb,limit", [
+    (10, 5, 5, 40 << 20),     # beta-column blocks of 64 columns
+    (10, 5, 4, 7 << 20),      # blocks of 32 columns (the narrowest)
+    (17, 2, 2, None),         # P = 153: two passes of output pairs, 3-group slicer
+    (17, 3, 2, 40 << 20)])    # both at once
+def test_blocks_and_passes(gpu, oracle, ozaki, norb, na, nb, limit):
+    from fqe_gb300 import _lib, synthetic
+    from fqe_gb300.fqe_data import ham_for
+    h1, h2, psi = synthetic.sector(norb, na, nb, 2 * norb, seed=norb + na)
+    d = gpu.FqeData(na, nb, norb)
+    d.set_wfn(strategy="from_data", raw_data=psi)
+    ham = ham_for(d._core, h1, h2)
+    if limit is not None:
+        _lib.call("fqegpu_ham_set_scratch_limit", ham.handle, limit)
+    out = d._run_apply(ham, alpha=0.5, beta=-0.25).cpu().numpy()
+    g = oracle.graph(norb, na, nb)
+    want = 0.5 * oracle.apply_spatial12(psi, h1, h2, g) - 0.25 * psi
+    err = numpy.linalg.norm(out - want) / numpy.linalg.norm(want)
+    assert err < TOL_OZ, err
