@@ -384,7 +384,9 @@ def run_gpu(args):
         "cpu_baseline": cpu,
     }
     if rank == 0 and world == 1 and not args.no_davidson:
-        line["davidson"] = davidson_leg(args.davidson_norb)
+        line["davidson"] = davidson_leg(args.davidson_norb, args.davidson_subspace,
+                                        args.davidson_scratch_gb,
+                                        args.davidson_max_iter)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -392,7 +394,7 @@ def run_gpu(args):
     return 0
 
 
-def davidson_leg(norb):
+def davidson_leg(norb, subspace=32, scratch_gb=None, max_iter=400):
     """Davidson to a 1e-6 residual on one sector, plain diagonal vs learned
     preconditioner, same GPU, same seeded synthetic integrals."""
     import torch
@@ -402,7 +404,8 @@ def davidson_leg(norb):
     nchol = synthetic.default_nchol(norb)
     h1, h2, _ = synthetic.integrals(norb, nchol, SEED)
     ham = fqe_gb300.RestrictedHamiltonian((h1, h2))
-    kw = dict(block=4, tol=1e-6, max_subspace=32, max_iter=400)
+    kw = dict(block=4, tol=1e-6, max_subspace=subspace, max_iter=max_iter,
+              scratch_limit=None if scratch_gb is None else int(scratch_gb * 2**30))
     dav.davidson(ham, na, nb, **dict(kw, max_iter=2))  # plans, tables, caches
     torch.cuda.synchronize()
 
@@ -416,7 +419,7 @@ def davidson_leg(norb):
 
     plain = dav.davidson(ham, na, nb, **kw)
     out = {"workload": f"lowest root, norb={norb} ({na}a,{nb}b), {nchol} "
-                       f"Cholesky vectors, seed {SEED}; block 4, subspace <= 32,"
+                       f"Cholesky vectors, seed {SEED}; block 4, subspace <= {subspace},"
                        " residual 1e-6",
            "plain": row(plain), "learned": None}
     if os.path.exists(precond.DEFAULT_WEIGHTS):
@@ -457,6 +460,10 @@ def main():
     ap.add_argument("--no-davidson", action="store_true",
                     help="skip the Davidson (plain vs learned) leg")
     ap.add_argument("--davidson-norb", type=int, default=12)
+    ap.add_argument("--davidson-subspace", type=int, default=32)
+    ap.add_argument("--davidson-scratch-gb", type=float, default=None,
+                    help="device workspace of the Davidson applies (GB)")
+    ap.add_argument("--davidson-max-iter", type=int, default=400)
     args = ap.parse_args()
     if args.norb != 14 or args.nalpha is not None or args.nbeta is not None:
         na = args.nalpha if args.nalpha is not None else args.norb // 2

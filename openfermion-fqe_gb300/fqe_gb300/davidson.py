@@ -128,13 +128,18 @@ class _Operator:
     """H on one sector: apply, diagonal (both include e_0)."""
 
     def __init__(self, hamiltonian: RestrictedHamiltonian, nalpha: int,
-                 nbeta: int, precision: Optional[str] = None):
+                 nbeta: int, precision: Optional[str] = None,
+                 scratch_limit: Optional[int] = None):
         tensors = hamiltonian.tensors()
         self.norb = hamiltonian.dim()
         self.graph = get_graph(nalpha, nbeta, self.norb)
         self.e0 = complex(hamiltonian.e_0())
         self.ham = ham_for(self.graph, tensors[0],
                            tensors[1] if len(tensors) > 1 else None)
+        if scratch_limit is not None:
+            # before the first apply: bounds the apply's device workspace
+            _lib.call("fqegpu_ham_set_scratch_limit", self.ham.handle,
+                      int(scratch_limit))
         self.shape = (self.graph.lena(), self.graph.lenb())
         self.precision = precision
         self.applies = 0
@@ -163,19 +168,22 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
              guess: Optional[List[torch.Tensor]] = None,
              preconditioner=None, precision: Optional[str] = None,
              verbose: bool = False, callback=None,
-             patience: int = 10) -> DavidsonResult:
+             patience: int = 10,
+             scratch_limit: Optional[int] = None) -> DavidsonResult:
     """Lowest `nroots` eigenpairs of the sector (nalpha, nbeta).
 
     `callback(iteration, ritz_vectors, residuals, ritz_values, operator)` is
     called once per iteration before the subspace is expanded (the learned
-    preconditioner's training samples are taken there).
+    preconditioner's training samples are taken there).  `scratch_limit`
+    bounds the apply's device workspace (bytes), leaving room for the
+    subspace vectors of large sectors.
 
     A preconditioner with a `plain` method (the learned one) is judged by the
     residual: when the largest residual of the wanted roots has not halved
     over `patience` iterations, the rest of the run uses the plain diagonal
     preconditioner (`fallback_iteration` records when)."""
     t_start = time.time()
-    op = _Operator(hamiltonian, nalpha, nbeta, precision)
+    op = _Operator(hamiltonian, nalpha, nbeta, precision, scratch_limit)
     block = max(nroots, block or nroots)
     if max_subspace < 2 * block:
         raise ValueError("max_subspace must hold at least two blocks")
