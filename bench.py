@@ -386,7 +386,7 @@ def run_gpu(args):
     if rank == 0 and world == 1 and not args.no_davidson:
         line["davidson"] = davidson_leg(args.davidson_norb, args.davidson_subspace,
                                         args.davidson_scratch_gb,
-                                        args.davidson_max_iter)
+                                        args.davidson_max_iter, prec)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -394,9 +394,11 @@ def run_gpu(args):
     return 0
 
 
-def davidson_leg(norb, subspace=32, scratch_gb=None, max_iter=400):
+def davidson_leg(norb, subspace=32, scratch_gb=None, max_iter=400,
+                 precision="ozaki", verbose=False):
     """Davidson to a 1e-6 residual on one sector, plain diagonal vs learned
-    preconditioner, same GPU, same seeded synthetic integrals."""
+    preconditioner, same GPU, same seeded synthetic integrals, applies in
+    `precision` ("ozaki": tensor cores, "fp64")."""
     import torch
     import fqe_gb300
     from fqe_gb300 import davidson as dav, precond, synthetic
@@ -405,6 +407,7 @@ def davidson_leg(norb, subspace=32, scratch_gb=None, max_iter=400):
     h1, h2, _ = synthetic.integrals(norb, nchol, SEED)
     ham = fqe_gb300.RestrictedHamiltonian((h1, h2))
     kw = dict(block=4, tol=1e-6, max_subspace=subspace, max_iter=max_iter,
+              precision=precision, verbose=verbose,
               scratch_limit=None if scratch_gb is None else int(scratch_gb * 2**30))
     dav.davidson(ham, na, nb, **dict(kw, max_iter=2))  # plans, tables, caches
     torch.cuda.synchronize()
@@ -420,7 +423,7 @@ def davidson_leg(norb, subspace=32, scratch_gb=None, max_iter=400):
     plain = dav.davidson(ham, na, nb, **kw)
     out = {"workload": f"lowest root, norb={norb} ({na}a,{nb}b), {nchol} "
                        f"Cholesky vectors, seed {SEED}; block 4, subspace <= {subspace},"
-                       " residual 1e-6",
+                       f" residual 1e-6, {precision} applies",
            "plain": row(plain), "learned": None}
     if os.path.exists(precond.DEFAULT_WEIGHTS):
         pre = precond.LearnedPreconditioner.load()

@@ -89,6 +89,11 @@ struct OzakiPlan {
   int32_t* d_tabTA = nullptr;          // [lena][KP] target tables, pair index fastest
   int32_t* d_tabTB = nullptr;          // [lenb][KP]
   __nv_bfloat16* d_dslices = nullptr;  // [tiles of a block][5][64 * KP] smem images
+  // beta-column blocks only: per block and target column, the pairs whose
+  // beta source lies in the block, CSR: offsets [nblk][lenb + 1], entries
+  // (pair, sign * (source - c0 + 1))
+  int32_t* d_boff = nullptr;
+  int2* d_bent = nullptr;
   int ring = 0;
   int nsm = 0;
   size_t smem = 0;
@@ -646,6 +651,57 @@ __device__ __forceinline__ double2 zmul2(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// Column-block scatter with the beta part read from the block's CSR list:
+// the alpha part only for targets inside the block (all pairs), the beta part
+// only for the (pair, source) entries whose source lies in the block.  Same
+// sums as k_oz_scatter over the same block, without scanning every pair of
+// every target once per block.
+__global__ void __launch_bounds__(256) k_oz_scatter_csr(
+    int P, int64_t lena, int64_t lenb, int64_t c0, int64_t w, int64_t gld,
+    const int32_t* __restrict__ tabA, const int32_t* __restrict__ boff,
+    const int2* __restrict__ bent, const float4* __restrict__ G,
+    const double2* __restrict__ psi, double2 alpha, double2 beta, int init,
+    double2* __restrict__ sigma) {
+  const int64_t a = blockIdx.y;
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= lenb) return;
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+  if (b >= c0 && b < c0 + w) {
+    for (int p = 0; p < P; ++p) {
+      const int32_t ca = tabA[(int64_t)p * lena + a];
+      if (ca) {
+        float4 g = G[((int64_t)p * lena + (abs(ca) - 1)) * gld + (b - c0)];
+        if (ca < 0) g = make_float4(-g.x, -g.y, -g.z, -g.w);
+        df_add(rh, rl, g.x, g.y);
+        df_add(ih, il, g.z, g.w);
+      }
+    }
+  }
+  const int32_t e1 = boff[b + 1];
+  for (int32_t e = boff[b]; e < e1; ++e) {
+    const int2 en = bent[e];
+    float4 g = G[((int64_t)en.x * lena + a) * gld + (abs(en.y) - 1)];
+    if (en.y < 0) g = make_float4(-g.x, -g.y, -g.z, -g.w);
+    df_add(rh, rl, g.x, g.y);
+    df_add(ih, il, g.z, g.w);
+  }
+  const int64_t I = a * lenb + b;
+  const double2 acc = make_double2((double)rh + (double)rl, (double)ih + (double)il);
+  double2 out = zmul2(alpha, acc);
+  if (init) {
+    if (beta.x != 0.0 || beta.y != 0.0) {
+      const double2 t = zmul2(beta, psi[I]);
+      out.x += t.x;
+      out.y += t.y;
+    }
+  } else {
+    const double2 s0 = sigma[I];
+    out.x += s0.x;
+    out.y += s0.y;
+  }
+  sigma[I] = out;
+}
+
 // sigma[I] (init: beta psi[I] +, else sigma[I] +) alpha * the contributions of
 // the beta-column block [c0, c0 + w) held in G ([P][lena][w]): the alpha part
 // of targets in the block, the beta part of every target whose source column
@@ -804,6 +860,41 @@ static int plan_create(fqegpu_ham h) {
     FQE_CUDA(cudaGetLastError());
     FQE_CUDA(cudaDeviceSynchronize());
   }
+  if (wb < lenb) {
+    // per block, for every target column, the (pair, source) entries whose
+    // beta source lies in the block, in pair order
+    const bool tri = h->compressed;
+    const int32_t* tb = tri ? h->g->b.tab_tri : h->g->b.tab_full;
+    std::vector<int32_t> tab((size_t)P * lenb);
+    FQE_CUDA(cudaMemcpy(tab.data(), tb, sizeof(int32_t) * tab.size(), cudaMemcpyDeviceToHost));
+    const int64_t nblk = (lenb + wb - 1) / wb;
+    const size_t row = (size_t)lenb + 1;
+    std::vector<int32_t> off((size_t)nblk * row, 0);
+    // counting sort by (block of the source, target column), pair order kept
+    for (int64_t b = 0; b < lenb; ++b)
+      for (int p = 0; p < P; ++p) {
+        const int32_t cb = tab[(size_t)p * lenb + b];
+        if (cb) ++off[(size_t)((std::abs(cb) - 1) / wb) * row + b + 1];
+      }
+    for (size_t i = 1; i < off.size(); ++i) off[i] += off[i - 1];  // [k][0] counts nothing
+    std::vector<int2> ent((size_t)off.back());
+    std::vector<int32_t> cur(off);
+    for (int64_t b = 0; b < lenb; ++b)
+      for (int p = 0; p < P; ++p) {
+        const int32_t cb = tab[(size_t)p * lenb + b];
+        if (!cb) continue;
+        const int64_t src = std::abs(cb) - 1, k = src / wb;
+        const int32_t v = (int32_t)(src - k * wb + 1);
+        ent[(size_t)cur[(size_t)k * row + b]++] = make_int2(p, cb > 0 ? v : -v);
+      }
+    FQE_CUDA(cudaMalloc(&pl->d_boff, sizeof(int32_t) * off.size()));
+    FQE_CUDA(cudaMemcpy(pl->d_boff, off.data(), sizeof(int32_t) * off.size(),
+                        cudaMemcpyHostToDevice));
+    FQE_CUDA(cudaMalloc(&pl->d_bent, sizeof(int2) * std::max<size_t>(ent.size(), 1)));
+    if (!ent.empty())
+      FQE_CUDA(cudaMemcpy(pl->d_bent, ent.data(), sizeof(int2) * ent.size(),
+                          cudaMemcpyHostToDevice));
+  }
   const int64_t ntiles = lena * ((wb + kDets - 1) / kDets);  // tiles of the widest block
   const int64_t npairs = (ntiles + 1) / 2;
   const size_t dsl = sizeof(__nv_bfloat16) * (size_t)npairs * 2 * kSlices * kN * KP;
@@ -840,6 +931,8 @@ void ozaki_destroy(fqegpu_ham h) {
   cudaFree(pl->d_tabTA);
   cudaFree(pl->d_tabTB);
   cudaFree(pl->d_dslices);
+  cudaFree(pl->d_boff);
+  cudaFree(pl->d_bent);
   delete pl;
   h->oz = nullptr;
 }
@@ -915,8 +1008,13 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
     }
     FQE_TRY(stage_mark(h, blk, 2, st));
     dim3 sg((unsigned)((lenb + 255) / 256), (unsigned)lena);
-    k_oz_scatter<<<sg, 256, 0, st>>>(pl->P, lena, lenb, c0, w, pl->wb, tabA, tabB, pl->d_G,
-                                     psi, al, beta, blk == 0 ? 1 : 0, sigma);
+    if (pl->d_boff)
+      k_oz_scatter_csr<<<sg, 256, 0, st>>>(pl->P, lena, lenb, c0, w, pl->wb, tabA,
+                                           pl->d_boff + (size_t)blk * (lenb + 1), pl->d_bent,
+                                           pl->d_G, psi, al, beta, blk == 0 ? 1 : 0, sigma);
+    else
+      k_oz_scatter<<<sg, 256, 0, st>>>(pl->P, lena, lenb, c0, w, pl->wb, tabA, tabB, pl->d_G,
+                                       psi, al, beta, blk == 0 ? 1 : 0, sigma);
     FQE_CUDA(cudaGetLastError());
     FQE_TRY(stage_mark(h, blk, 3, st));
   }

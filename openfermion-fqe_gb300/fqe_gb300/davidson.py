@@ -51,7 +51,7 @@ class DiagonalPreconditioner:
 
 
 class _PlainOf:
-    """The plain preconditioner of a learned one (after the judge's switch)."""
+    """The plain preconditioner of a learned one (after the residual guard switched)."""
 
     name = "diagonal"
 
@@ -178,7 +178,7 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
     bounds the apply's device workspace (bytes), leaving room for the
     subspace vectors of large sectors.
 
-    A preconditioner with a `plain` method (the learned one) is judged by the
+    A preconditioner with a `plain` method (the learned one) is watched by the
     residual: when the largest residual of the wanted roots has not halved
     over `patience` iterations, the rest of the run uses the plain diagonal
     preconditioner (`fallback_iteration` records when)."""

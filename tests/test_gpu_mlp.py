@@ -176,7 +176,7 @@ def test_trained_network_gain(gpu):
     # What the shipped network (trained on norb 10-12 correction equations,
     # fqe_gb300/data/precond_mlp.npz) gains over the plain preconditioner on
     # held-out sectors: a lower correction-equation loss, the objective it was
-    # trained on.  Davidson with it, judged by the residual with the plain
+    # trained on.  Davidson with it, watched by the residual guard with the plain
     # fallback, converges to the plain run's energy; the iteration counts are
     # printed, not asserted (on these synthetic integrals the learned
     # multiplier costs iterations).
