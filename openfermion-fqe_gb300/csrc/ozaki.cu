@@ -429,75 +429,90 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       }
     }
   } else if (warp == kMmaWarp) {
-    if (lane == 0) {
-      const uint32_t idesc = tc::make_idesc_bf16(kM, (uint32_t)NP);
-      const uint32_t sbo = (uint32_t)KP * 16u;          // V: full-K rows
-      const uint32_t sbo_c = (uint32_t)kChunkK * 16u;   // D chunk: 16-column rows
-      // B = V slice descriptors of k-step 0; k-step ks adds 256 bytes = 16 units
-      uint64_t vdesc0[kSlices];
-      for (int a = 0; a < kSlices; ++a)
-        vdesc0[a] = tc::make_sdesc(tc::smem_u32(sV + (size_t)a * v_elems), 128, sbo);
-      int64_t it = 0;
-      int slot = 0;
-      uint32_t ph = 0;
-      for (int64_t t = t_begin; t < t_end; ++t, ++it) {
-        if (!oz_wait(accempty, (uint32_t)((it & 1) ^ 1), abort_flag)) {
-          oz_abort(abort_flag, A.err, 2);
-          break;
-        }
-        tc::fence_after_sync();
-        uint32_t fresh = (1u << kAccs) - 1u;  // accumulators not yet written
-        bool ok = true;
-        // chunk group (b, gi): up to four 16-column K chunks of D slice b; a
-        // slot is released as soon as its MMAs complete
-        for (int b = 1; b <= kSlices && ok; ++b) {
-          const int amax = min(kSlices, kMaxLevel - b);
-          for (int gi = 0; gi < ngr; ++gi) {
-            const int c0 = gi * kGroupK;
-            const int nk = min(kGroupK, nch - c0);
-            if (!oz_wait(&full[slot], ph, abort_flag)) {
-              oz_abort(abort_flag, A.err, 3);
-              ok = false;
-              break;
-            }
-            tc::fence_after_sync();
-            const uint64_t dd =
-                tc::make_sdesc(tc::smem_u32(sD + (size_t)slot * slot_elems), 128, sbo_c);
-            // k-step outer, V slice inner: consecutive MMAs go to different
-            // accumulators (measured faster than runs into one accumulator)
+    // The whole warp runs the issue loop, so descriptors and counters stay
+    // warp-uniform; lane 0 alone issues the MMAs and commits.  Levels,
+    // accumulators and accumulate flags are compile-time after unrolling b,
+    // c and a: the issue loop is the contraction's limit, not the tensor pipe.
+    const uint32_t elect = lane == 0 ? 1u : 0u;
+    const uint32_t idesc = tc::make_idesc_bf16(kM, (uint32_t)NP);
+    const uint32_t sbo = (uint32_t)KP * 16u;          // V: full-K rows
+    const uint32_t sbo_c = (uint32_t)kChunkK * 16u;   // D chunk: 16-column rows
+    // B = V slice descriptors of k-step 0; k-step ks adds 256 bytes = 16 units
+    uint64_t vdesc0[kSlices];
 #pragma unroll
-            for (int c = 0; c < kGroupK; ++c) {
-              if (c < nk) {
+    for (int a = 0; a < kSlices; ++a)
+      vdesc0[a] = tc::make_sdesc(tc::smem_u32(sV + (size_t)a * v_elems), 128, sbo);
+    uint32_t accs[kAccs];
 #pragma unroll
-                for (int a = 1; a <= kSlices; ++a) {
-                  if (a <= amax) {
-                    const int lvl = a + b;
-                    const int ai = lvl <= 4 ? lvl - 2 : 3;
-                    const uint32_t acc = tmem + (uint32_t)(ai * NP);
-                    // A (D chunk) advances one 4 KB pair chunk = 256 units per
-                    // k-step; B (V slice a) advances 256 bytes = 16 units
-                    tc::mma_bf16(acc, dd + (uint64_t)(256 * c),
-                                 vdesc0[a - 1] + (uint64_t)(16 * (c0 + c)), idesc,
-                                 (fresh >> ai) & 1u ? 0u : 1u);
-                    fresh &= ~(1u << ai);
-                  }
+    for (int i = 0; i < kAccs; ++i) accs[i] = tmem + (uint32_t)(i * NP);
+    const uint32_t sD0 = tc::smem_u32(sD);
+    int64_t it = 0;
+    int slot = 0;
+    uint32_t ph = 0;
+    bool ok = true;
+    for (int64_t t = t_begin; t < t_end && ok; ++t, ++it) {
+      // warp-uniform outcome of every wait
+      if (!__all_sync(0xffffffffu, oz_wait(accempty, (uint32_t)((it & 1) ^ 1), abort_flag))) {
+        if (elect) oz_abort(abort_flag, A.err, 2);
+        ok = false;
+        break;
+      }
+      tc::fence_after_sync();
+      // chunk group (b, gi): up to four 16-column K chunks of D slice b; a
+      // slot is released as soon as its MMAs complete
+#pragma unroll
+      for (int b = 1; b <= kSlices; ++b) {
+        for (int gi = 0; gi < ngr && ok; ++gi) {
+          const int c0 = gi * kGroupK;
+          const int nk = min(kGroupK, nch - c0);
+          if (!__all_sync(0xffffffffu, oz_wait(&full[slot], ph, abort_flag))) {
+            if (elect) oz_abort(abort_flag, A.err, 3);
+            ok = false;
+            break;
+          }
+          tc::fence_after_sync();
+          const uint64_t dd = tc::make_sdesc(sD0 + (uint32_t)slot * slot_elems * 2u, 128, sbo_c);
+          // k-step outer, V slice inner: consecutive MMAs go to different
+          // accumulators
+#pragma unroll
+          for (int c = 0; c < kGroupK; ++c) {
+            if (c < nk) {
+              // A (D chunk) advances one 4 KB pair chunk = 256 units per
+              // k-step; B (V slice a) advances 256 bytes = 16 units
+              const uint64_t da = dd + (uint64_t)(256 * c);
+              const uint64_t kb = (uint64_t)(16 * (c0 + c));
+              // the first MMA into each accumulator of the tile pair
+              // (b = 1, first chunk, a <= 4) overwrites it
+              const uint32_t first = (gi == 0 && c == 0) ? 1u : 0u;
+#pragma unroll
+              for (int a = 1; a <= kSlices; ++a) {
+                if (a + b <= kMaxLevel) {
+                  const int lvl = a + b;
+                  const int ai = lvl <= 4 ? lvl - 2 : 3;
+                  const uint32_t accum = (b == 1 && a <= 4) ? (first ^ 1u) : 1u;
+                  tc::mma_bf16_if(accs[ai], da, vdesc0[a - 1] + kb, idesc, accum, elect);
                 }
               }
             }
-            tc::mma_commit(&empty[slot]);
-            if (++slot == R) {
-              slot = 0;
-              ph ^= 1u;
-            }
+          }
+          if (elect) tc::mma_commit(&empty[slot]);
+          __syncwarp();
+          if (++slot == R) {
+            slot = 0;
+            ph ^= 1u;
           }
         }
-        if (!ok) break;
-        tc::mma_commit(accfull);
       }
-      // every MMA issued above has completed before TMEM is released
+      if (!ok) break;
+      if (elect) tc::mma_commit(accfull);
+      __syncwarp();
+    }
+    // every MMA issued above has completed before TMEM is released
+    if (elect) {
       tc::mma_commit(done);
       if (!oz_wait(done, 0, abort_flag) && !*abort_flag) oz_abort(abort_flag, A.err, 6);
     }
+    __syncwarp();
   } else {
     const int quarter = warp & 3, cg = warp >> 2;
     const int row = 32 * quarter + lane;      // TMEM lane = MMA row
@@ -528,46 +543,60 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       }
       tc::fence_after_sync();
       const uint32_t base = tmem + ((uint32_t)(32 * quarter) << 16);
-      // this lane's half of G[p][det]: (hi, lo) of the real or imaginary part
-      float2* gcol = reinterpret_cast<float2*>(A.G + ia * A.gld + (ib - A.c0)) + part;
-      const int64_t pstride = A.lena * A.gld * 2;  // float2 elements per pair row
-      for (int c0 = 0; c0 < cw; c0 += 4) {
-        const int pc = pbeg + c0;
-        uint32_t ra[4], rb[4], rc[4], rd[4];
-        tc::tmem_ld4_nowait(base + (uint32_t)pc, ra);
-        tc::tmem_ld4_nowait(base + (uint32_t)(NP + pc), rb);
-        tc::tmem_ld4_nowait(base + (uint32_t)(2 * NP + pc), rc);
-        tc::tmem_ld4_nowait(base + (uint32_t)(3 * NP + pc), rd);
-        tc::tmem_wait_ld();
-        if (!live) continue;
+      // drain TMEM first: the four level sums of every column of this warp's
+      // group, combined into an FP32 pair (exact two-sum of levels 2 and 3,
+      // then levels 4 and 5..7), scaled, and held in registers; the
+      // accumulators are released before the G stores, so the next tile
+      // pair's MMAs run while this one's G goes out
+      const int colexp = bits - 62 + g0;  // |D| < 2^colexp in this column
+      float hreg[kM / 4], lreg[kM / 4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int p = A.p0 + pc + k;
-          if (p >= A.P) break;
-          // column exponent: |D| < 2^(bits - 62 + g0); row exponent of V
-          const int sc = sVexp[pc + k] + bits - 62 + g0;
-          const float x = __uint_as_float(ra[k]), y = __uint_as_float(rb[k]);
-          // exact two-sum of levels 2 and 3, then levels 4 and 5..7
-          const float h = x + y;
-          const float bb = h - x;
-          float l = (x - (h - bb)) + (y - bb);
-          l += __uint_as_float(rc[k]);
-          l += __uint_as_float(rd[k]);
-          const float h2 = h + l;
-          const float l2 = l - (h2 - h);
-          float2 o;
-          if (sc >= -126 && sc <= 127) {
-            const float f = pow2f(sc);
-            o = make_float2(h2 * f, l2 * f);
-          } else {
-            o = make_float2(scale2(h2, sc), scale2(l2, sc));
+      for (int c0 = 0; c0 < kM / 4; c0 += 4) {
+        if (c0 < cw) {
+          const int pc = pbeg + c0;
+          uint32_t ra[4], rb[4], rc[4], rd[4];
+          tc::tmem_ld4_nowait(base + (uint32_t)pc, ra);
+          tc::tmem_ld4_nowait(base + (uint32_t)(NP + pc), rb);
+          tc::tmem_ld4_nowait(base + (uint32_t)(2 * NP + pc), rc);
+          tc::tmem_ld4_nowait(base + (uint32_t)(3 * NP + pc), rd);
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const float x = __uint_as_float(ra[k]), y = __uint_as_float(rb[k]);
+            const float h = x + y;
+            const float bb = h - x;
+            float l = (x - (h - bb)) + (y - bb);
+            l += __uint_as_float(rc[k]);
+            l += __uint_as_float(rd[k]);
+            const float h2 = h + l;
+            const float l2 = l - (h2 - h);
+            // with the row exponent of V
+            const int sc = sVexp[pc + k] + colexp;
+            if (sc >= -126 && sc <= 127) {
+              const float f = pow2f(sc);
+              hreg[c0 + k] = h2 * f;
+              lreg[c0 + k] = l2 * f;
+            } else {
+              hreg[c0 + k] = scale2(h2, sc);
+              lreg[c0 + k] = scale2(l2, sc);
+            }
           }
-          gcol[(int64_t)p * pstride] = o;
         }
       }
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(accempty);
+      if (!live) continue;
+      // this lane's half of G[p][det]: (hi, lo) of the real or imaginary part
+      const int64_t pstride = A.lena * A.gld * 2;  // float2 elements per pair row
+      float2* gp = reinterpret_cast<float2*>(A.G + ia * A.gld + (ib - A.c0)) + part +
+                   (int64_t)(A.p0 + pbeg) * pstride;
+      const int nst = min(cw, A.P - A.p0 - pbeg);  // columns holding real pairs
+#pragma unroll
+      for (int c = 0; c < kM / 4; ++c) {
+        if (c < nst) *gp = make_float2(hreg[c], lreg[c]);
+        gp += pstride;
+      }
     }
   }
   tc::fence_before_sync();

@@ -84,6 +84,20 @@ __device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc,
       : "memory");
 }
 
+// mma_bf16 issued only where `issue` is nonzero: a whole warp runs the issue
+// loop (its descriptors and counters stay warp-uniform) and one lane issues.
+__device__ __forceinline__ void mma_bf16_if(uint32_t dtmem, uint64_t adesc,
+                                            uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate, uint32_t issue) {
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "setp.ne.b32 q, %5, 0;\n\t"
+      "@q tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(dtmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate), "r"(issue)
+      : "memory");
+}
+
 // Arrive (once) on an mbarrier when all prior tcgen05 async operations of the
 // issuing thread complete.
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
