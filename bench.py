@@ -331,6 +331,13 @@ def run_gpu(args):
         ntiles = d.lena() * ((d.lenb() + 31) // 32)
         images = 2 * ((ntiles + 1) // 2) * 5 * 64 * KP * 2.0
         traffic = 0.98 * (images + 16.0 * P * n)
+    elif prec == "ozaki" and names[dom] == "gather":
+        # k_oz_slice DRAM bytes per launch: the norb-12 capture measured 1.386 GB
+        # (0.073 read + 1.313 written) for 1.372 GB of slice images = 1.01 x
+        # the images it writes; scaled to this workload's images (the small
+        # exponent and fixed-point pre-passes of the stage are not included)
+        ntiles = d.lena() * ((d.lenb() + 31) // 32)
+        traffic = 1.01 * 2 * ((ntiles + 1) // 2) * 5 * 64 * KP * 2.0
     roofline = {"kernel": names[dom], "bound": dk["bound"],
                 "achieved": dk["achieved"], "peak": dk["peak"],
                 "unit": dk["unit"],

@@ -32,11 +32,12 @@
 //               tile pair interleaved chunk by chunk).
 //   k_oz_mma    persistent, one CTA per SM: a loader lane streams the slice
 //               images with cp.async.bulk into a ring of 16 KB slots (four K
-//               chunks of a tile pair each); one thread issues 128 x 128 x 16
-//               tcgen05.mma (A = V slices resident in shared memory, B = 64
-//               determinants); sixteen epilogue warps combine the four
-//               accumulators (single-buffered, 512 TMEM columns) into G,
-//               stored as FP32 pairs [P][lena][lenb] with 32-byte stores.
+//               chunks of a tile pair each); the MMA warp runs the issue
+//               loop and lane 0 issues 128 x NP x 16 tcgen05.mma (A = 64
+//               determinants x re/im of the streamed chunk, B = V slices
+//               resident in shared memory); sixteen epilogue warps combine
+//               the four accumulators (single-buffered, 4 x NP TMEM columns)
+//               into G, stored coalesced as FP32 pairs [P][lena][w].
 //   k_oz_scatter  sigma from G in FP32-pair arithmetic (k_oz_rowexp,
 //               k_oz_globalexp and k_oz_fixed prepare the fixed-point psi).
 // Every wait in k_oz_mma is bounded; on a timeout the kernel records an
