@@ -444,6 +444,86 @@ def davidson_leg(norb, subspace=32, scratch_gb=None, max_iter=400,
     return out
 
 
+def configs_leg():
+    """The benchmark's other single-GPU configurations, measured once each on
+    their seeded synthetic inputs (CUDA events on the current stream):
+    norb 8 (4a,4b) one apply and a Taylor step t = 0.05 to 1e-12; norb 14
+    (7a,7b) FP64 vs tensor-core apply (relative error), a diagonal-Coulomb
+    evolve t = 0.1 (V ~ N(0, 0.5) symmetric) and a Taylor step t = 0.05 to
+    1e-12 on both paths (relative error, norm)."""
+    import numpy
+    import torch
+    import fqe_gb300
+    from fqe_gb300 import settings, synthetic
+
+    def timed(fn, reps=1):
+        torch.cuda.synchronize()
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(reps):
+            r = fn()
+        e.record()
+        torch.cuda.synchronize()
+        return r, s.elapsed_time(e) / reps
+
+    def wfn(norb, na, nb, psi):
+        w = fqe_gb300.Wavefunction([[na + nb, na - nb, norb]])
+        w.set_wfn(strategy="from_data", raw_data={(na + nb, na - nb): psi})
+        return w
+
+    def rel(a, b):
+        return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+
+    old = settings.precision
+    out = {}
+    try:
+        settings.precision = "fp64"
+        h1, h2, psi = synthetic.sector(8, 4, 4, synthetic.default_nchol(8), SEED)
+        ham = fqe_gb300.RestrictedHamiltonian((h1, h2))
+        w = wfn(8, 4, 4, psi)
+        w.apply(ham)
+        _, t_ap = timed(lambda: w.apply(ham), 20)
+        w.apply_generated_unitary(0.05, "taylor", ham, accuracy=1e-12, expansion=80)
+        ev, t_ev = timed(lambda: w.apply_generated_unitary(
+            0.05, "taylor", ham, accuracy=1e-12, expansion=80))
+        out["norb8_fp64"] = {"apply_ms": t_ap, "taylor_ms": t_ev,
+                             "taylor_terms": ev._taylor_terms,
+                             "taylor_norm": float(torch.linalg.norm(ev.get_coeff((8, 0))))}
+
+        norb, na, nb = 14, 7, 7
+        key = (na + nb, na - nb)
+        h1, h2, psi = synthetic.sector(norb, na, nb, synthetic.default_nchol(norb), SEED)
+        ham = fqe_gb300.RestrictedHamiltonian((h1, h2))
+        w = wfn(norb, na, nb, psi)
+        row = {}
+        res = {}
+        for prec in ("fp64", "ozaki"):
+            settings.precision = prec
+            w.apply(ham)
+            s, t_ap = timed(lambda: w.apply(ham), 3)
+            ev, t_ev = timed(lambda: w.apply_generated_unitary(
+                0.05, "taylor", ham, accuracy=1e-12, expansion=80))
+            res[prec] = (s.get_coeff(key), ev.get_coeff(key))
+            row[prec] = {"apply_ms": t_ap, "taylor_ms": t_ev,
+                         "taylor_terms": ev._taylor_terms,
+                         "taylor_norm": float(torch.linalg.norm(ev.get_coeff(key)))}
+        row["apply_rel_err_ozaki_vs_fp64"] = rel(res["ozaki"][0], res["fp64"][0])
+        row["taylor_rel_err_ozaki_vs_fp64"] = rel(res["ozaki"][1], res["fp64"][1])
+        settings.precision = "fp64"
+        dc = fqe_gb300.get_diagonalcoulomb_hamiltonian(synthetic.diagonal_coulomb(norb, SEED))
+        w.time_evolve(0.1, dc, inplace=True)
+        _, t_dc = timed(lambda: w.time_evolve(0.1, dc, inplace=True), 10)
+        n = psi.size
+        row["diag_coulomb_evolve"] = {
+            "ms": t_dc, "gbs": 32.0 * n / (t_dc / 1e3) / 1e9,
+            "norm_after_11_steps": float(torch.linalg.norm(w.get_coeff(key)))}
+        out["norb14"] = row
+    finally:
+        settings.precision = old
+    return out
+
+
 def _block_w(ham):
     import numpy
     from fqe_gb300 import _lib
@@ -474,6 +554,10 @@ def main():
     ap.add_argument("--davidson-scratch-gb", type=float, default=None,
                     help="device workspace of the Davidson applies (GB)")
     ap.add_argument("--davidson-max-iter", type=int, default=400)
+    ap.add_argument("--configs", action="store_true",
+                    help="only measure the other single-GPU configurations "
+                         "(norb 8 apply/Taylor; norb 14 FP64 vs tensor-core "
+                         "error, Taylor, diagonal-Coulomb evolve)")
     args = ap.parse_args()
     if args.norb != 14 or args.nalpha is not None or args.nbeta is not None:
         na = args.nalpha if args.nalpha is not None else args.norb // 2
@@ -483,6 +567,13 @@ def main():
                      args.nchol or synthetic.default_nchol(args.norb))
     if args.impl == "reference":
         return run_reference(args)
+    if args.configs:
+        import torch
+        import fqe_gb300
+        torch.cuda.set_device(0)
+        fqe_gb300.build()
+        print(json.dumps({"configs": configs_leg()}), flush=True)
+        return 0
     return run_gpu(args)
 
 

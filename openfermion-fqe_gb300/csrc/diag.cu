@@ -72,7 +72,12 @@ __global__ void k_string_terms(int norb, int64_t len,
   out[s] = EXP ? zexp(f) : f;
 }
 
-// One CTA per alpha string; threads over beta strings.
+// One CTA per alpha string; threads over beta strings.  The evolve (mode 0)
+// with norb <= 16 splits the beta string into a low half of h orbitals and a
+// high half: per CTA, tlo[m] = exp(f(a)) prod_{k in m} exp(row_a[k]) and
+// thi[m] = prod_{k in m} exp(row_a[h + k]) (built by doubling), so a
+// determinant costs three complex products instead of one per beta electron
+// (FP64 is the limit of this kernel on GB300).
 template <int MODE>
 __global__ void __launch_bounds__(256) k_diag_apply(
     int norb, int64_t lena, int64_t lenb, const uint64_t* __restrict__ astr,
@@ -80,6 +85,7 @@ __global__ void __launch_bounds__(256) k_diag_apply(
     const double2* __restrict__ fa, const double2* __restrict__ fb,
     double2* __restrict__ psi, double* __restrict__ diag_out) {
   __shared__ double2 row[kMaxOrb];
+  __shared__ double2 tlo[256], thi[256];
   const int64_t a = blockIdx.x;
   const uint64_t Sa = astr[a];
   for (int k = threadIdx.x; k < norb; k += blockDim.x) {
@@ -93,6 +99,28 @@ __global__ void __launch_bounds__(256) k_diag_apply(
   }
   __syncthreads();
   const double2 fav = fa[a];
+  if (MODE == 0 && norb <= 16) {
+    const int h = (norb + 1) / 2, hh = norb - h;  // both <= 8
+    if (threadIdx.x == 0) {
+      tlo[0] = fav;
+      thi[0] = make_double2(1.0, 0.0);
+    }
+    __syncthreads();
+    for (int j = 0; j < 8; ++j) {
+      const int w = 1 << j, t = threadIdx.x;  // entries [w, 2w) from [0, w)
+      if (j < h && t < w) tlo[w + t] = zmul(tlo[t], row[j]);
+      if (j < hh && t < w) thi[w + t] = zmul(thi[t], row[h + j]);
+      __syncthreads();
+    }
+    const uint64_t lomask = (1ull << h) - 1ull;
+    for (int64_t b = threadIdx.x; b < lenb; b += blockDim.x) {
+      const uint64_t Sb = bstr[b];
+      const int64_t I = a * lenb + b;
+      const double2 p = zmul(zmul(tlo[Sb & lomask], thi[Sb >> h]), fb[b]);
+      psi[I] = zmul(psi[I], p);
+    }
+    return;
+  }
   for (int64_t b = threadIdx.x; b < lenb; b += blockDim.x) {
     const uint64_t Sb = bstr[b];
     const int64_t I = a * lenb + b;
