@@ -59,3 +59,31 @@ def test_reference_arm_other_ranks_do_nothing(monkeypatch, capsys):
         gpus, steps, warmup = 2, 1, 0
     assert bench.run_reference(Args()) == 0
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line_on_rank0(monkeypatch, capsys):
+    """Rank 0 of the reference arm times the oracle port (small sector here)
+    and prints one line with the reference-arm keys."""
+    import json
+    sys.path.insert(0, REPO)
+    import bench
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    saved = (bench.NORB, bench.NALPHA, bench.NBETA, bench.NCHOL, bench.METRIC)
+    bench.set_workload(8, 4, 4, 16)
+
+    class Args:
+        gpus, steps, warmup = 1, 1, 0
+    try:
+        assert bench.run_reference(Args()) == 0
+    finally:
+        bench.NORB, bench.NALPHA, bench.NBETA, bench.NCHOL, bench.METRIC = saved
+    lines = [x for x in capsys.readouterr().out.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["unit"] == "det/s"
+    assert line["config"]["determinants"] == 70 * 70
+    assert line["value"] > 0 and line["cpu_baseline"]["value"] == line["value"]
+    assert line["cpu_baseline"]["kind"] == "port"
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["e2e"]["d2h_bytes_per_step"] == 0
