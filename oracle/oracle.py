@@ -325,6 +325,23 @@ def dense_hamiltonian(h1, h2, g: Graph):
     return H
 
 
+def rdm12(ket, g: Graph, bra=None):
+    """FqeData.rdm12(bradata) with ket = self, half-filling form
+    (fqe_data.py:1762-1781): with D[i, j, I] = <I|E_ij|.>,
+    raw[k, l, i, j] = sum_I conj(D_bra[k, l, I]) D_ket[i, j, I],
+    rdm2 = -raw.transpose(1, 2, 0, 3) and rdm2[:, i, i, :] += rdm1; rdm1 as
+    rdm1() (= <bra|E_ij|ket>)."""
+    bra = ket if bra is None else bra
+    dket = make_dvec(ket, g)
+    dbra = dket if bra is ket else make_dvec(bra, g)
+    r1 = numpy.tensordot(dket, numpy.conj(bra), axes=((2, 3), (0, 1)))
+    raw = numpy.tensordot(numpy.conj(dbra), dket, axes=((2, 3), (2, 3)))
+    r2 = -raw.transpose(1, 2, 0, 3)
+    for i in range(g.norb):
+        r2[:, i, i, :] += r1
+    return r1, r2
+
+
 def rdm1(ket, g: Graph, bra=None):
     """FqeData.rdm1(bradata) with ket = self (fqe_data.py:1668-1724):
     rdm1[i][j] = <bra| E_ij |ket> = sum_I conj(bra_I) dvec_ket[i, j, I]."""

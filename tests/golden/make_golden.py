@@ -239,8 +239,45 @@ def rdm_fixture():
     save("rdm", **out)
 
 
+def rdm12_fixture():
+    """FqeData.rdm12 of the reference (fqe_data.py:1726-1760): the half-filling
+    branch (blocked and plain numpy, :1762-1838) and the low-filling branch
+    (C and python, :1840-2033), each with and without a bra (transition RDMs)."""
+    out = {}
+    for norb, na, nb, seed in [(4, 2, 1, 0), (5, 2, 2, 1), (6, 3, 2, 2),
+                               (8, 2, 1, 3), (7, 1, 2, 4)]:
+        rng = numpy.random.default_rng(6000 + seed)
+        ket = FqeData(na, nb, norb)
+        bra = FqeData(na, nb, norb)
+        ket.coeff = synthetic.wavefunction_coeff(ket.lena(), ket.lenb(), rng)
+        bra.coeff = synthetic.wavefunction_coeff(bra.lena(), bra.lenb(), rng)
+        tag = f"{norb}_{na}_{nb}"
+        out[f"ket_{tag}"] = ket.coeff.copy()
+        out[f"bra_{tag}"] = bra.coeff.copy()
+        # the filling threshold is fixed when an FqeData is made: objects
+        # made with the accelerated switch on always take the half-filling
+        # branch; objects made with it off take the low-filling branch below
+        # 30 % filling (C or python by the switch at call time)
+        for made, called, suffix in ((True, True, ""), (False, False, "py"),
+                                     (False, True, "c")):
+            fqe.settings.use_accelerated_code = made
+            k2 = FqeData(na, nb, norb)
+            b2 = FqeData(na, nb, norb)
+            k2.coeff = ket.coeff.copy()
+            b2.coeff = bra.coeff.copy()
+            fqe.settings.use_accelerated_code = called
+            r1, r2 = k2.rdm12()
+            t1, t2 = k2.rdm12(b2)
+            out[f"rdm1{suffix}_{tag}"] = r1
+            out[f"rdm2{suffix}_{tag}"] = r2
+            out[f"trdm1{suffix}_{tag}"] = t1
+            out[f"trdm2{suffix}_{tag}"] = t2
+        fqe.settings.use_accelerated_code = True
+    save("rdm12", **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["graph", "apply", "dc", "taylor", "dvec",
-                             "davidson", "rdm"]
+                             "davidson", "rdm", "rdm12"]
     for name in which:
         globals()[name + "_fixture"]()
