@@ -1,5 +1,6 @@
-"""One-particle RDM (FqeData.rdm1, fqe_data.py:1668-1724) on the GPU against
-the reference's own outputs (tests/golden/rdm.npz) and the oracle."""
+"""One- and two-particle RDMs (FqeData.rdm1, fqe_data.py:1668-1724;
+FqeData.rdm12, :1726-1838) on the GPU against the reference's own outputs
+(tests/golden/rdm.npz, rdm12.npz) and the oracle."""
 
 import numpy
 import pytest
@@ -54,3 +55,22 @@ def test_rdm1_sector_mismatch(gpu):
     b = gpu.FqeData(2, 1, 4)
     with pytest.raises(ValueError):
         a.rdm1(b)
+
+
+def test_rdm12_matches_reference(gpu, golden):
+    # FqeData.rdm12 (fqe_data.py:1726-1838) against the reference's
+    # half-filling branch, with and without a bra (tests/golden/rdm12.npz)
+    gd = golden("rdm12")
+    for key in [k for k in gd if k.startswith("rdm2_")]:
+        tag = key[5:]
+        norb, na, nb = map(int, tag.split("_"))
+        ket = _data(gpu, norb, na, nb, gd["ket_" + tag])
+        bra = _data(gpu, norb, na, nb, gd["bra_" + tag])
+        r1, r2 = ket.rdm12()
+        numpy.testing.assert_allclose(r1, gd["rdm1_" + tag], atol=TOL, rtol=0)
+        numpy.testing.assert_allclose(r2, gd["rdm2_" + tag], atol=TOL, rtol=0)
+        t1, t2 = ket.rdm12(bra)
+        numpy.testing.assert_allclose(t1, gd["trdm1_" + tag], atol=TOL, rtol=0)
+        numpy.testing.assert_allclose(t2, gd["trdm2_" + tag], atol=TOL, rtol=0)
+    with pytest.raises(ValueError):
+        gpu.FqeData(2, 2, 4).rdm12(gpu.FqeData(2, 1, 4))

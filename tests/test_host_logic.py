@@ -90,3 +90,24 @@ def test_no_cpu_fallback_without_device():
         pytest.skip("a device is present")
     with pytest.raises(RuntimeError):
         settings.device()
+
+
+def test_rdm2_assembly_matches_reference_fixture(golden, oracle):
+    # FqeData.rdm12's host-side assembly (GEMM of the dvecs, permutation,
+    # rdm1 on the diagonal), run on CPU tensors with the oracle's dvecs
+    import torch
+    from fqe_gb300.fqe_data import rdm2_from_dvecs
+    gd = golden("rdm12")
+    for key in [k for k in gd if k.startswith("rdm2_")]:
+        tag = key[5:]
+        norb, na, nb = map(int, tag.split("_"))
+        g = oracle.graph(norb, na, nb)
+        ket, bra = gd["ket_" + tag], gd["bra_" + tag]
+        dket = torch.from_numpy(oracle.make_dvec(ket, g))
+        dbra = torch.from_numpy(oracle.make_dvec(bra, g))
+        r1 = torch.from_numpy(oracle.rdm1(ket, g))
+        r2 = rdm2_from_dvecs(dket, dket, r1).numpy()
+        assert numpy.abs(r2 - gd["rdm2_" + tag]).max() < 1e-13
+        t1 = torch.from_numpy(oracle.rdm1(ket, g, bra))
+        t2 = rdm2_from_dvecs(dket, dbra, t1).numpy()
+        assert numpy.abs(t2 - gd["trdm2_" + tag]).max() < 1e-13
