@@ -17,8 +17,12 @@ reference keeps in Python:
 * ``make_dvec`` / ``make_coeff``  fqe_data.py:2209-2234, 2309-2334
 * ``rdm1``                        FqeData.rdm1 / _rdm1_blocked (fqe_data.py:1668-1724):
                                   rdm1[i][j] = <bra|E_ij|ket> through make_dvec
+* ``rdm12``                       FqeData.rdm12, half-filling form (fqe_data.py:1762-1838)
 * ``diagonal_energies``           <I|H|I> for a restricted Hamiltonian, by
                                   applying H to unit vectors (small cases only)
+
+``ozaki_model.py`` beside it models this project's tensor-core contraction
+arithmetic in numpy (no reference counterpart) for tests/test_ozaki_model.py.
 
 Used by tests/ (as the checker), by ``__graft_entry__.smoke`` and by
 bench.py's CPU legs.  Its parity with the reference is pinned by

@@ -1,0 +1,75 @@
+"""The numerical design of the tensor-core (Ozaki-split BF16) contraction,
+checked on the CPU with the numpy model oracle/ozaki_model.py (five 8-bit
+slices of 40-bit fixed point per operand, 19 products a + b <= 7, four FP32
+level accumulators, two-sum combination): the level sums 2-4 are exact, and
+the contraction and the apply stay within the 1e-10 relative bound the GPU
+tests hold the kernel to.  The same design's device results are compared
+with the oracle in tests/test_gpu_ozaki.py."""
+
+import numpy
+import pytest
+
+
+def _rel(a, b):
+    return numpy.linalg.norm(a - b) / numpy.linalg.norm(b)
+
+
+def _case(oracle, norb, na, nb, seed, peaked=False):
+    import ozaki_model as om
+    from fqe_gb300 import synthetic
+    h1, h2, psi = synthetic.sector(norb, na, nb, 2 * norb, seed)
+    if peaked:
+        rng = numpy.random.default_rng(seed)
+        psi = 1e-6 * (rng.normal(size=psi.shape) + 1j * rng.normal(size=psi.shape))
+        psi[0, 0] = 0.99
+        psi[-1, 1] = -0.1j
+    g = oracle.graph(norb, na, nb)
+    V = om.pair_matrix(h1, h2, na + nb, oracle.prep_spatial12)
+    assert numpy.abs(V.imag).max() == 0.0  # real integrals: the tensor-core form
+    D = oracle.make_dvec(psi, g).reshape(norb * norb, -1)
+    return h1, h2, psi, g, V.real.copy(), D
+
+
+def test_levels_2_to_4_are_exact(oracle):
+    import ozaki_model as om
+    *_, V, D = _case(oracle, 8, 4, 4, 3)
+    Dr = numpy.concatenate([D.real, D.imag], axis=1)
+    a32, _, _ = om.level_sums(V, Dr, fp32=True)
+    a64, _, _ = om.level_sums(V, Dr, fp32=False)
+    for lvl in range(3):  # levels 2, 3, 4
+        assert numpy.array_equal(a32[lvl].astype(numpy.float64), a64[lvl])
+    # levels 5..7 share one accumulator and round, far below level 2's scale
+    assert numpy.abs(a32[3] - a64[3]).max() <= 2.0 ** -40 * numpy.abs(a64[0]).max()
+
+
+@pytest.mark.parametrize("norb,na,nb,peaked", [(8, 4, 4, False), (8, 3, 5, False),
+                                               (10, 3, 3, False), (8, 4, 4, True)])
+def test_contraction_and_apply_within_bound(oracle, norb, na, nb, peaked):
+    import ozaki_model as om
+    h1, h2, psi, g, V, D = _case(oracle, norb, na, nb, norb + na, peaked)
+    G64 = V @ D
+    G = om.contract(V, D)
+    assert _rel(G, G64) < 1e-11  # measured 2-3e-12
+    shape = (norb, norb, g.lena, g.lenb)
+    ref = oracle.apply_spatial12(psi, h1, h2, g)
+    # the FP64 dvec form is the reference's apply ...
+    assert _rel(oracle.make_coeff(G64.reshape(shape), g), ref) < 1e-12
+    # ... and the modelled tensor-core contraction stays well within the
+    # 1e-10 bound (measured 3-4e-12, as the kernel on the GPU)
+    assert _rel(oracle.make_coeff(G.reshape(shape), g), ref) < 1e-11
+
+
+def test_fewer_slices_would_break_the_bound(oracle):
+    # the design's margin: stopping the products at level 5 instead of 7
+    # leaves an error far above 1e-10
+    import ozaki_model as om
+    *_, V, D = _case(oracle, 8, 4, 4, 5)
+    Dr = numpy.concatenate([D.real, D.imag], axis=1)
+    old = om.MAX_LEVEL
+    try:
+        om.MAX_LEVEL = 5
+        acc, er, ec = om.level_sums(V, Dr)
+        G5 = om.combine(acc, er, ec)
+    finally:
+        om.MAX_LEVEL = old
+    assert _rel(G5, V @ Dr) > 1e-9
