@@ -9,6 +9,8 @@ reference keeps in Python:
 * ``prep_spatial12``              h1'/h2' preparation (fqe_data.py:691-693)
 * ``apply_spatial12``             _apply_array_spatial12_lm (fqe_data.py:685-710)
 * ``apply_spatial1``              dense_apply_array_spatial1 (fqe_data.py:497-526)
+* ``apply_spin1`` / ``apply_spin12``  spin-orbital operators (fqe_data.py:533-563,
+                                  743-773): the same kernels with spin blocks
 * ``apply_restricted``            Wavefunction._apply_array (wavefunction.py:366-399)
 * ``taylor_evolve``               apply_generated_unitary, Taylor branch
                                   (wavefunction.py:553-568, 605-606)
@@ -214,6 +216,59 @@ def apply_spatial1(coeff, h1, g: Graph):
         if dexc.shape[1] and coeff.size:
             _check(L.orc_apply1(_p(coeff), _p(out), _p(dexc), g.lena, g.lenb,
                                 dexc.shape[1], _p(h1c), is_alpha), "apply1")
+    return out
+
+
+def apply_spin1(coeff, h1, g: Graph):
+    """sigma for a spin-orbital one-body operator h1 [2n, 2n] (alpha orbitals
+    first): the alpha block on alpha strings, the beta block on beta strings
+    (fqe_data.py:533-563, lm branch :551-563)."""
+    L = lib()
+    n = g.norb
+    h1 = numpy.asarray(h1, dtype=numpy.complex128)
+    coeff = numpy.ascontiguousarray(coeff, dtype=numpy.complex128)
+    out = numpy.zeros_like(coeff)
+    for is_alpha, dexc, blk in ((1, g.dexca, h1[:n, :n]), (0, g.dexcb, h1[n:, n:])):
+        if dexc.shape[1] and coeff.size:
+            hb = numpy.ascontiguousarray(blk)
+            _check(L.orc_apply1(_p(coeff), _p(out), _p(dexc), g.lena, g.lenb,
+                                dexc.shape[1], _p(hb), is_alpha), "apply1 spin")
+    return out
+
+
+def apply_spin12(coeff, h1, h2, g: Graph):
+    """sigma for spin-orbital one- and two-body operators h1 [2n, 2n], h2
+    [2n]^4 (alpha orbitals first), as _apply_array_spin12_lm
+    (fqe_data.py:743-773): the h1'/h2' preparation over all 2n orbitals, the
+    same-spin kernel with the alpha-alpha blocks on alpha strings and the
+    beta-beta blocks on beta strings, and the opposite-spin kernel with
+    h2'[a,a,b,b] + h2'[b,b,a,a] transposed to (k l i j)."""
+    L = lib()
+    n = g.norb
+    h1p, h2p = prep_spatial12(h1, h2)  # the same preparation, over 2n orbitals
+    coeff = numpy.ascontiguousarray(coeff, dtype=numpy.complex128)
+    out = numpy.zeros_like(coeff)
+    if coeff.size == 0 or n == 0:
+        return out
+    nda = g.dexca.shape[1]
+    ndb = g.dexcb.shape[1]
+    a, b = slice(0, n), slice(n, 2 * n)
+    if nda:
+        _check(L.orc_apply12_same_spin(
+            _p(coeff), _p(out), _p(g.dexca), g.lena, g.lenb, nda,
+            _p(numpy.ascontiguousarray(h1p[a, a])),
+            _p(numpy.ascontiguousarray(h2p[a, a, a, a])), n, 1), "spin same alpha")
+    if ndb:
+        _check(L.orc_apply12_same_spin(
+            _p(coeff), _p(out), _p(g.dexcb), g.lena, g.lenb, ndb,
+            _p(numpy.ascontiguousarray(h1p[b, b])),
+            _p(numpy.ascontiguousarray(h2p[b, b, b, b])), n, 0), "spin same beta")
+    if nda and ndb:
+        h2ab = numpy.ascontiguousarray(
+            h2p[a, a, b, b] + numpy.einsum("ijkl->klij", h2p[b, b, a, a]))
+        _check(L.orc_apply12_diff_spin(_p(coeff), _p(out), _p(g.dexca),
+                                       _p(g.dexcb), g.lena, g.lenb, nda, ndb,
+                                       _p(h2ab), n), "spin diff")
     return out
 
 

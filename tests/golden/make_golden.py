@@ -276,8 +276,30 @@ def rdm12_fixture():
     save("rdm12", **out)
 
 
+def spin_fixture():
+    """FqeData.apply with spin-orbital operators (fqe_data.py:404-470 ->
+    _apply_array_spin1 :533-608, _apply_array_spin12 :610-635): random
+    complex h1 [2n, 2n] and h2 [2n]^4, alpha orbitals first."""
+    out = {}
+    for norb, na, nb, seed in [(4, 2, 2, 0), (5, 2, 1, 1), (5, 2, 3, 2),
+                               (4, 0, 2, 3), (4, 3, 1, 4)]:
+        rng = numpy.random.default_rng(7000 + seed)
+        d = FqeData(na, nb, norb)
+        d.coeff = synthetic.wavefunction_coeff(d.lena(), d.lenb(), rng)
+        m = 2 * norb
+        h1 = rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m))
+        h2 = rng.normal(size=(m,) * 4) + 1j * rng.normal(size=(m,) * 4)
+        tag = f"{norb}_{na}_{nb}"
+        out[f"psi_{tag}"] = d.coeff.copy()
+        out[f"h1_{tag}"] = h1
+        out[f"h2_{tag}"] = h2
+        out[f"spin1_{tag}"] = d.apply((h1,)).coeff
+        out[f"spin12_{tag}"] = d.apply((h1, h2)).coeff
+    save("spin", **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["graph", "apply", "dc", "taylor", "dvec",
-                             "davidson", "rdm", "rdm12"]
+                             "davidson", "rdm", "rdm12", "spin"]
     for name in which:
         globals()[name + "_fixture"]()

@@ -257,3 +257,33 @@ def test_rdm12_matches_fixture(golden, oracle):
         # with d gives -(N - 1) rdm1[a, c]
         ne = na + nb
         assert numpy.abs(numpy.einsum("ikjk->ij", r2) + (ne - 1) * r1).max() < 1e-12
+
+
+def test_spin_orbital_apply_matches_fixture(golden, oracle):
+    # FqeData.apply with spin-orbital (2n-dimensional) one- and two-body
+    # operators, the reference's own outputs
+    gd = golden("spin")
+    for key in [k for k in gd if k.startswith("spin12_")]:
+        tag = key[7:]
+        norb, na, nb = map(int, tag.split("_"))
+        g = oracle.graph(norb, na, nb)
+        psi, h1, h2 = gd["psi_" + tag], gd["h1_" + tag], gd["h2_" + tag]
+        out1 = oracle.apply_spin1(psi, h1, g)
+        assert numpy.abs(out1 - gd["spin1_" + tag]).max() < 1e-12
+        out12 = oracle.apply_spin12(psi, h1, h2, g)
+        scale = max(1.0, numpy.abs(gd[key]).max())
+        assert numpy.abs(out12 - gd[key]).max() < 1e-12 * scale
+    # a spin-free operator written in spin orbitals is the spatial apply
+    norb, na, nb = 4, 2, 1
+    g = oracle.graph(norb, na, nb)
+    rng = numpy.random.default_rng(3)
+    h1 = rng.normal(size=(norb, norb))
+    h2 = rng.normal(size=(norb,) * 4)
+    psi = rng.normal(size=(g.lena, g.lenb)) + 0j
+    H1 = numpy.kron(numpy.eye(2), h1)
+    H2 = numpy.zeros((2 * norb,) * 4)
+    for s in (slice(0, norb), slice(norb, 2 * norb)):
+        for t in (slice(0, norb), slice(norb, 2 * norb)):
+            H2[s, t, s, t] = h2
+    want = oracle.apply_spatial12(psi, h1, h2, g)
+    assert numpy.abs(oracle.apply_spin12(psi, H1, H2, g) - want).max() < 1e-12
