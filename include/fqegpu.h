@@ -15,6 +15,11 @@
  *   - Handles (graph, hamiltonian, workspace) own their device memory and are
  *     released with the matching *_destroy call.
  *
+ * Ordering: a Hamiltonian handle owns one apply's workspace (dvec blocks,
+ * tensor-core plan, staging buffer), so calls on the same handle must be
+ * ordered (one stream, or synchronised between streams); different handles
+ * and graphs are independent and may run on different streams or threads.
+ *
  * Errors: every entry point returns an fqegpu_status; nothing exits, traps or
  * prints.  The text of the last error of the calling thread is available from
  * fqegpu_last_error().  The reference instead exits from safe_malloc
