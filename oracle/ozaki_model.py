@@ -53,12 +53,14 @@ def slices(x, e):
     return out
 
 
-def level_sums(V, D, fp32=True):
+def level_sums(V, D, fp32=True, e_col=None):
     """The four level accumulators of G = V D for real V [P, K], D [K, M]:
     returns (acc [4, P, M], e_row [P], e_col [M]).  With fp32=False the
-    accumulation runs in float64 (to show where FP32 rounds)."""
+    accumulation runs in float64 (to show where FP32 rounds); `e_col`
+    replaces the exact column exponents by given upper bounds."""
     e_row = _exponents(V, 1)
-    e_col = _exponents(D, 0)
+    if e_col is None:
+        e_col = _exponents(D, 0)
     vs = slices(V, e_row[:, None])
     ds = slices(D, e_col[None, :])
     dt = numpy.float32 if fp32 else numpy.float64
@@ -91,11 +93,23 @@ def combine(acc, e_row, e_col):
     return (h2.astype(numpy.float64) + l2.astype(numpy.float64)) * scale
 
 
-def contract(V, D):
+def psi_bound_exponents(psi):
+    """Per-determinant exponent bounds from psi alone: every D[q][a, b] is a
+    sum of at most one psi entry of column b (alpha source) and one of row a
+    (beta source), so |D| < 2^(max(rowexp(a), colexp(b)) + 1)."""
+    ex = numpy.frexp(numpy.maximum(numpy.abs(psi.real), numpy.abs(psi.imag)))[1]
+    eb = numpy.maximum(ex.max(axis=1)[:, None], ex.max(axis=0)[None, :]) + 1
+    return eb.ravel()
+
+
+def contract(V, D, e_det=None):
     """The modelled tensor-core G = V D for real V [P, K] and complex D [K, N]
-    (real and imaginary columns side by side, as on the device)."""
+    (real and imaginary columns side by side, as on the device).  `e_det`
+    [N] replaces the exact per-column exponents by per-determinant bounds
+    (for both the real and the imaginary column)."""
     Dr = numpy.concatenate([D.real, D.imag], axis=1)
-    acc, e_row, e_col = level_sums(V, Dr)
+    e_col = None if e_det is None else numpy.concatenate([e_det, e_det])
+    acc, e_row, e_col = level_sums(V, Dr, e_col=e_col)
     G = combine(acc, e_row, e_col)
     n = D.shape[1]
     return G[:, :n] + 1j * G[:, n:]
