@@ -298,8 +298,62 @@ def spin_fixture():
     save("spin", **out)
 
 
+def wfn_pickles_fixture():
+    """The reference's own Wavefunction.apply golden data
+    (tests/unittest_data/wavefunction/*.pickle, checked by
+    tests/wavefunction_test.py:609-627): the restricted-Hamiltonian
+    ('apply_array' with a RestrictedHamiltonian) and diagonal-Coulomb
+    ('apply_dc') cases of the number-conserving wavefunctions, unpacked per
+    sector into plain arrays."""
+    import pickle
+    from fqe.hamiltonians.restricted_hamiltonian import RestrictedHamiltonian
+    src = os.path.join(ref_fqe.REF_ROOT, "tests", "unittest_data", "wavefunction")
+    out = {}
+    for f in sorted(os.listdir(src)):
+        if not f.endswith(".pickle"):
+            continue
+        with open(os.path.join(src, f), "rb") as fh:
+            data = pickle.load(fh)
+        if not isinstance(data, dict) or "wfn" not in data:
+            continue
+        name = f[:-len(".pickle")].replace("-", "m")
+        wfn = data["wfn"]
+        if not wfn.conserve_number():
+            # number-broken wavefunctions (the XX files) go through the
+            # reference's beta-inversion (wavefunction.py:337-359): not on
+            # this path
+            continue
+        norb = wfn.norb()
+        cases = []
+        arr = data.get("apply_array")
+        if arr and isinstance(arr["hamil"], RestrictedHamiltonian) \
+                and arr["wfn_out"] is not None:
+            cases.append(("array", arr))
+        dc = data.get("apply_dc")
+        if dc and dc["wfn_out"] is not None:
+            cases.append(("dc", dc))
+        for kind, case in cases:
+            ham = case["hamil"]
+            tag = f"{name}_{kind}"
+            out[f"norb_{tag}"] = numpy.array(norb)
+            out[f"e0_{tag}"] = numpy.array(complex(ham.e_0()))
+            if kind == "array":
+                for r, t in enumerate(ham.tensors()):
+                    out[f"t{r}_{tag}"] = numpy.asarray(t, dtype=numpy.complex128)
+            else:
+                out[f"diag_{tag}"] = numpy.asarray(ham._tensor[1], dtype=numpy.complex128)
+                out[f"vij_{tag}"] = numpy.asarray(ham._tensor[2], dtype=numpy.complex128)
+            for key in wfn.sectors():
+                nele, sz = key
+                na, nb = (nele + sz) // 2, (nele - sz) // 2
+                sec = f"{tag}_{na}_{nb}"
+                out[f"psi_{sec}"] = wfn.get_coeff(key).copy()
+                out[f"out_{sec}"] = case["wfn_out"].get_coeff(key).copy()
+    save("wfn_pickles", **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["graph", "apply", "dc", "taylor", "dvec",
-                             "davidson", "rdm", "rdm12", "spin"]
+                             "davidson", "rdm", "rdm12", "spin", "wfn_pickles"]
     for name in which:
         globals()[name + "_fixture"]()

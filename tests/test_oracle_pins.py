@@ -287,3 +287,29 @@ def test_spin_orbital_apply_matches_fixture(golden, oracle):
             H2[s, t, s, t] = h2
     want = oracle.apply_spatial12(psi, h1, h2, g)
     assert numpy.abs(oracle.apply_spin12(psi, H1, H2, g) - want).max() < 1e-12
+
+
+def test_reference_wavefunction_pickles(golden, oracle):
+    # the reference's own Wavefunction.apply golden data
+    # (tests/unittest_data/wavefunction/*.pickle, wavefunction_test.py:609-627),
+    # unpacked by tests/golden/make_golden.py: restricted Hamiltonians
+    # ('apply_array') and diagonal Coulomb ('apply_dc'), every sector
+    gd = golden("wfn_pickles")
+    n = 0
+    for key in [k for k in gd if k.startswith("out_")]:
+        name, kind, na, nb = key[4:].rsplit("_", 3)
+        tag = f"{name}_{kind}"
+        norb = int(gd["norb_" + tag])
+        g = oracle.graph(norb, int(na), int(nb))
+        psi = gd[f"psi_{tag}_{na}_{nb}"]
+        e0 = complex(gd["e0_" + tag])
+        if kind == "array":
+            out = oracle.apply_restricted(psi, (gd["t0_" + tag], gd["t1_" + tag]), e0, g)
+        else:
+            out = oracle.apply_diagonal_coulomb(psi, gd["diag_" + tag], gd["vij_" + tag], g)
+            if abs(e0) > 1e-15:
+                out = out + e0 * psi
+        want = gd[key]
+        assert numpy.abs(out - want).max() <= 1e-12 * max(1.0, numpy.abs(want).max())
+        n += 1
+    assert n >= 15
