@@ -316,3 +316,29 @@ def test_apply_deterministic(gpu):
     a = d.apply((h1, h2)).to_numpy()
     b = d.apply((h1, h2)).to_numpy()
     assert numpy.array_equal(a, b)
+
+
+def test_reference_wavefunction_pickles(gpu, golden):
+    # the reference's own Wavefunction.apply golden data (restricted
+    # Hamiltonians with e_0, diagonal Coulomb), every sector, FP64 path
+    gd = golden("wfn_pickles")
+    for key in [k for k in gd if k.startswith("out_")]:
+        name, kind, na, nb = key[4:].rsplit("_", 3)
+        tag = f"{name}_{kind}"
+        norb, na, nb = int(gd["norb_" + tag]), int(na), int(nb)
+        psi = gd[f"psi_{tag}_{na}_{nb}"]
+        e0 = complex(gd["e0_" + tag])
+        want = gd[key]
+        if kind == "array":
+            wfn = gpu.Wavefunction([[na + nb, na - nb, norb]])
+            wfn.set_wfn(strategy="from_data", raw_data={(na + nb, na - nb): psi})
+            ham = gpu.get_restricted_hamiltonian((gd["t0_" + tag], gd["t1_" + tag]),
+                                                 e_0=e0)
+            out = wfn.apply(ham).get_coeff((na + nb, na - nb)).cpu().numpy()
+        else:
+            d = _sector(gpu, norb, na, nb, psi)
+            out = d.apply_diagonal_coulomb(gd["diag_" + tag],
+                                           gd["vij_" + tag]).cpu().numpy()
+            if abs(e0) > 1e-15:
+                out = out + e0 * psi
+        assert numpy.abs(out - want).max() <= TOL_FP64 * max(1.0, numpy.abs(want).max())
