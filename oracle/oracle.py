@@ -11,6 +11,9 @@ reference keeps in Python:
 * ``apply_spatial1``              dense_apply_array_spatial1 (fqe_data.py:497-526)
 * ``apply_spin1`` / ``apply_spin12``  spin-orbital operators (fqe_data.py:533-563,
                                   743-773): the same kernels with spin blocks
+* ``transform_orbitals``          an orbital map on a sector through compound
+                                  matrices (the result of Wavefunction.transform,
+                                  wavefunction.py:813-959, by another route)
 * ``apply_restricted``            Wavefunction._apply_array (wavefunction.py:366-399)
 * ``taylor_evolve``               apply_generated_unitary, Taylor branch
                                   (wavefunction.py:553-568, 605-606)
@@ -270,6 +273,30 @@ def apply_spin12(coeff, h1, h2, g: Graph):
                                        _p(g.dexcb), g.lena, g.lenb, nda, ndb,
                                        _p(h2ab), n), "spin diff")
     return out
+
+
+def compound_matrix(M, strings, norb):
+    """C[J][I] = det M[occ(J), occ(I)]: the action of the one-particle map M
+    on the determinants of one spin (strings in the graph's order)."""
+    occ = [[k for k in range(norb) if (int(s) >> k) & 1] for s in strings]
+    n = len(occ)
+    C = numpy.ones((n, n), dtype=numpy.complex128)  # no electrons: det of 0x0
+    if n and occ[0]:
+        for J in range(n):
+            for I in range(n):
+                C[J, I] = numpy.linalg.det(M[numpy.ix_(occ[J], occ[I])])
+    return C
+
+
+def transform_orbitals(coeff, m_alpha, m_beta, g: Graph):
+    """The sector under the orbital maps m_alpha, m_beta [norb, norb]:
+    coeff' = C_alpha coeff C_beta^T with C the compound matrices.  The
+    reference's Wavefunction.transform (wavefunction.py:813-959) applies
+    M = P^T U^H, where P L U = U^H is scipy's LU of the rotation's adjoint,
+    through recursive column operators (fqe_data.py:1476-1535)."""
+    A = compound_matrix(numpy.asarray(m_alpha), g.astr, g.norb)
+    B = compound_matrix(numpy.asarray(m_beta), g.bstr, g.norb)
+    return A @ numpy.asarray(coeff, dtype=numpy.complex128) @ B.T
 
 
 def apply_restricted(coeff, tensors, e_0, g: Graph):

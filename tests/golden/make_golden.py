@@ -352,8 +352,47 @@ def wfn_pickles_fixture():
     save("wfn_pickles", **out)
 
 
+def transform_fixture():
+    """Wavefunction.transform (wavefunction.py:813-959) with spatial (norb)
+    and block-diagonal spin-orbital (2 norb) rotations, some close to a
+    permutation so that the LU inside pivots; records the rotation, the
+    returned permutation and the transformed sector."""
+    from scipy.stats import unitary_group
+    out = {}
+    cases = [(4, 2, 1, 0, False, False), (5, 2, 2, 1, True, False),
+             (6, 3, 2, 2, False, True), (5, 3, 1, 3, True, True),
+             (4, 0, 2, 4, False, False)]
+    for norb, na, nb, seed, near_perm, spin in cases:
+        rng = numpy.random.default_rng(8000 + seed)
+
+        def rot(k):
+            u = unitary_group.rvs(norb, random_state=100 * seed + k)
+            if near_perm:
+                q = numpy.eye(norb)[rng.permutation(norb)]
+                u, _ = numpy.linalg.qr(0.05 * u + q)
+            return u
+        if spin:
+            U = numpy.zeros((2 * norb, 2 * norb), dtype=numpy.complex128)
+            U[:norb, :norb] = rot(0)
+            U[norb:, norb:] = rot(1)
+        else:
+            U = rot(0)
+        w = fqe.Wavefunction([[na + nb, na - nb, norb]])
+        lena, lenb = math.comb(norb, na), math.comb(norb, nb)
+        psi = synthetic.wavefunction_coeff(lena, lenb, rng)
+        w.set_wfn(strategy="from_data", raw_data={(na + nb, na - nb): psi.copy()})
+        perm, _, _, res = w.transform(U)
+        tag = f"{norb}_{na}_{nb}_{seed}"
+        out[f"psi_{tag}"] = psi
+        out[f"rot_{tag}"] = U
+        out[f"perm_{tag}"] = perm
+        out[f"out_{tag}"] = res.get_coeff((na + nb, na - nb)).copy()
+    save("transform", **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["graph", "apply", "dc", "taylor", "dvec",
-                             "davidson", "rdm", "rdm12", "spin", "wfn_pickles"]
+                             "davidson", "rdm", "rdm12", "spin", "wfn_pickles",
+                             "transform"]
     for name in which:
         globals()[name + "_fixture"]()

@@ -313,3 +313,26 @@ def test_reference_wavefunction_pickles(golden, oracle):
         assert numpy.abs(out - want).max() <= 1e-12 * max(1.0, numpy.abs(want).max())
         n += 1
     assert n >= 15
+
+
+def test_orbital_transform_matches_fixture(golden, oracle):
+    # Wavefunction.transform of the reference (wavefunction.py:813-959): with
+    # P L U = U^H (scipy's LU of the rotation's adjoint, P returned), the
+    # sector is mapped by M = P^T U^H — here through compound matrices, an
+    # independent route to the reference's recursive column operators
+    gd = golden("transform")
+    n = 0
+    for key in [k for k in gd if k.startswith("out_")]:
+        tag = key[4:]
+        norb, na, nb, _ = map(int, tag.split("_"))
+        g = oracle.graph(norb, na, nb)
+        U, P = gd["rot_" + tag], gd["perm_" + tag]
+        M = P.T @ U.conj().T
+        if U.shape[0] == norb:
+            ma = mb = M
+        else:
+            ma, mb = M[:norb, :norb], M[norb:, norb:]
+        out = oracle.transform_orbitals(gd["psi_" + tag], ma, mb, g)
+        assert numpy.abs(out - gd[key]).max() < 1e-12
+        n += 1
+    assert n == 5
