@@ -17,6 +17,7 @@ reference keeps in Python:
 * ``apply_restricted``            Wavefunction._apply_array (wavefunction.py:366-399)
 * ``taylor_evolve``               apply_generated_unitary, Taylor branch
                                   (wavefunction.py:553-568, 605-606)
+* ``chebyshev_evolve``            the same, Chebyshev branch (:570-606)
 * ``evolve_diagonal_coulomb`` / ``apply_diagonal_coulomb``
                                   fqe_data.py:263-361 -> lib/fqe_data.c:455-602
 * ``make_dvec`` / ``make_coeff``  fqe_data.py:2209-2234, 2309-2334
@@ -331,6 +332,41 @@ def taylor_evolve(coeff, tensors, e_0, time, g: Graph, accuracy=1.0e-15,
     if abs(e_0 * time) > 1.0e-15:
         result *= numpy.exp(-1.0j * time * e_0)
     return result, order
+
+
+def chebyshev_evolve(coeff, tensors, e_0, time, g: Graph, spec_lim,
+                     accuracy=1.0e-15, expansion=30):
+    """apply_generated_unitary, Chebyshev branch (wavefunction.py:570-602)
+    plus the e_0 phase (:605-606), on one sector: with a = (E1 - E0) /
+    (2 w'), w' = 0.9875, and shift s = -(E0 + a w'), the series
+    exp(-i t (H + s)) = J0(a t) + sum_k 2 (-i)^k J_k(a t) T_k((H + s) / a)
+    summed until |T_k psi| |c_k| < accuracy, times exp(i s t) and, for
+    e_0 != 0, exp(-i t e_0) (the operator H includes e_0)."""
+    from scipy.special import jv
+    psi = numpy.asarray(coeff, dtype=numpy.complex128)
+    w = 0.9875
+    a = (spec_lim[1] - spec_lim[0]) / (2.0 * w)
+    shift = -(spec_lim[0] + a * w)
+
+    def h_scaled(v):  # (H + shift) v / a
+        return (apply_restricted(v, tensors, e_0, g) + shift * v) / a
+
+    t_prev = psi.copy()
+    t_cur = h_scaled(psi)
+    out = jv(0, a * time) * psi + 2.0 * jv(1, a * time) * (-1j) * t_cur
+    for k in range(2, expansion):
+        t_next = 2.0 * h_scaled(t_cur) - t_prev
+        t_prev, t_cur = t_cur, t_next
+        c = 2.0 * jv(k, a * time) * (-1j) ** k
+        out = out + c * t_cur
+        if numpy.linalg.norm(t_cur) * abs(c) < accuracy:
+            break
+    else:
+        raise RuntimeError("maximum chebyshev expansion limit reached")
+    out = out * numpy.exp(shift * time * 1j)
+    if abs(e_0 * time) > 1.0e-15:
+        out = out * numpy.exp(-1j * time * e_0)
+    return out
 
 
 def evolve_diagonal_coulomb(coeff, diag, vij, g: Graph):

@@ -390,9 +390,41 @@ def transform_fixture():
     save("transform", **out)
 
 
+def chebyshev_fixture():
+    """Wavefunction.apply_generated_unitary(time, 'chebyshev', ...)
+    (wavefunction.py:570-606) for restricted Hamiltonians with and without
+    e_0, spectral limits from the dense spectrum widened by 5 %."""
+    from fqe.hamiltonians.restricted_hamiltonian import RestrictedHamiltonian
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    out = {}
+    for norb, na, nb, seed, e0, t in [(4, 2, 1, 0, 0.0, 0.3), (5, 2, 2, 1, 0.7 - 0.2j, 0.25),
+                                       (6, 3, 2, 2, 0.0, 0.1)]:
+        h1, h2, psi = synthetic.sector(norb, na, nb, 2 * norb, seed)
+        g = oracle.graph(norb, na, nb)
+        H = oracle.dense_hamiltonian(h1, h2, g)
+        w = numpy.linalg.eigvalsh(0.5 * (H + H.conj().T))
+        pad = 0.05 * (w[-1] - w[0])
+        lim = [float(w[0] - pad), float(w[-1] + pad)]
+        ham = RestrictedHamiltonian((h1, h2), e_0=e0)
+        wfn = fqe.Wavefunction([[na + nb, na - nb, norb]])
+        wfn.set_wfn(strategy="from_data", raw_data={(na + nb, na - nb): psi.copy()})
+        res = wfn.apply_generated_unitary(t, "chebyshev", ham, accuracy=1e-13,
+                                          expansion=200, spec_lim=lim)
+        tag = f"{norb}_{na}_{nb}"
+        out[f"psi_{tag}"] = psi
+        out[f"h1_{tag}"] = h1
+        out[f"h2_{tag}"] = h2
+        out[f"e0_{tag}"] = numpy.array(complex(e0))
+        out[f"t_{tag}"] = numpy.array(t)
+        out[f"lim_{tag}"] = numpy.array(lim)
+        out[f"out_{tag}"] = res.get_coeff((na + nb, na - nb)).copy()
+    save("chebyshev", **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["graph", "apply", "dc", "taylor", "dvec",
                              "davidson", "rdm", "rdm12", "spin", "wfn_pickles",
-                             "transform"]
+                             "transform", "chebyshev"]
     for name in which:
         globals()[name + "_fixture"]()

@@ -336,3 +336,21 @@ def test_orbital_transform_matches_fixture(golden, oracle):
         assert numpy.abs(out - gd[key]).max() < 1e-12
         n += 1
     assert n == 5
+
+
+def test_chebyshev_matches_fixture(golden, oracle):
+    # apply_generated_unitary(..., 'chebyshev', ...) of the reference
+    gd = golden("chebyshev")
+    for key in [k for k in gd if k.startswith("out_")]:
+        tag = key[4:]
+        norb, na, nb = map(int, tag.split("_"))
+        g = oracle.graph(norb, na, nb)
+        out = oracle.chebyshev_evolve(gd["psi_" + tag], (gd["h1_" + tag], gd["h2_" + tag]),
+                                      complex(gd["e0_" + tag]), float(gd["t_" + tag]), g,
+                                      list(gd["lim_" + tag]), accuracy=1e-13,
+                                      expansion=200)
+        assert numpy.abs(out - gd[key]).max() < 1e-12
+        # unitary but for e_0's imaginary part, whose phase the reference
+        # applies twice (inside H and again at the end)
+        e0, t = complex(gd["e0_" + tag]), float(gd["t_" + tag])
+        assert abs(numpy.linalg.norm(out) - numpy.exp(2 * t * e0.imag)) < 1e-11
