@@ -291,7 +291,7 @@ def run_gpu(args):
     P = ham.npairs
     lena = d.lena()
     hbm_peak, bf16_peak, peak_src = peaks()
-    flops_fp64_peak = 1.10  # TFLOP/s, GB300 DGEMM probed with torch on this machine
+    flops_fp64_peak = 1.10  # TFLOP/s, GB300 DGEMM measured with torch (float64 matmul)
     # algorithmic work per apply (contraction: 2 real GEMMs of
     # P x P x N; gather writes and scatter reads D/G at 16 B per element)
     KP = (P + 15) // 16 * 16
@@ -346,7 +346,7 @@ def run_gpu(args):
                 "traffic_source": "ncu capture at norb 12 scaled by algorithmic bytes"
                 if traffic else None,
                 "peak_source": peak_src if dk["bound"] != "fp64"
-                else "torch float64 matmul 4096^3 on a GB300 of this pool"}
+                else "torch float64 matmul 4096^3 on a GB300"}
     # whole-apply HBM view with the uncompressed dvec byte model 16 norb^2 + 32
     alg_bytes = (16.0 * NORB * NORB + 32.0) * n
     apply_hbm = {"bytes_per_det": 16 * NORB * NORB + 32,

@@ -40,7 +40,7 @@ typedef enum {
   FQEGPU_ERR_INVALID = 1,     /* bad shape / argument (reference: ValueError) */
   FQEGPU_ERR_NOMEM = 2,       /* device or host allocation failed            */
   FQEGPU_ERR_CUDA = 3,        /* CUDA runtime error (text in last_error)     */
-  FQEGPU_ERR_UNSUPPORTED = 4, /* valid request this build does not handle    */
+  FQEGPU_ERR_UNSUPPORTED = 4, /* valid request this library does not handle  */
   FQEGPU_ERR_TIMEOUT = 5,     /* a bounded device wait gave up               */
   FQEGPU_ERR_NUMERIC = 6,     /* non-finite value or series did not converge */
 } fqegpu_status;
@@ -104,7 +104,7 @@ int fqegpu_ham_destroy(fqegpu_ham h);
  * of one apply at the current block width. */
 int fqegpu_ham_info(fqegpu_ham h, int64_t *info4);
 /* Upper bound on device scratch one apply may hold (default: 40% of free
- * memory at creation).  Smaller budgets stream narrower beta-column blocks. */
+ * memory at creation).  Smaller limits stream narrower beta-column blocks. */
 int fqegpu_ham_set_scratch_limit(fqegpu_ham h, int64_t bytes);
 
 /* Per-stage device time of the last apply on this handle (milliseconds,

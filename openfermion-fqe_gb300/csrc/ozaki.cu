@@ -863,7 +863,7 @@ static int plan_create(fqegpu_ham h) {
                       cudaMemcpyHostToDevice));
   const int64_t lena = h->g->a.len, lenb = h->g->b.len, N = lena * lenb;
   // beta-column blocks: slice images (20 KP bytes) and G (16 P bytes) per
-  // determinant of a block within the handle's scratch budget
+  // determinant of a block within the handle's scratch limit
   const int64_t per_col = (int64_t)(20 * KP + 16 * P) * lena;
   int64_t wb = h->scratch_limit / std::max<int64_t>(per_col, 1);
   if (wb >= lenb) {

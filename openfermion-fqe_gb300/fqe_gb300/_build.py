@@ -3,7 +3,7 @@
 Each translation unit under ``csrc/`` is compiled in parallel with
 ``nvcc -gencode arch=compute_103a,code=sm_103a -lineinfo -O3`` and linked into
 ``fqe_gb300/libfqegpu.so`` next to this file.  The CUDA runtime is linked
-statically, so the library depends only on the driver.
+statically, so the library depends only on the CUDA driver library (libcuda).
 """
 
 import concurrent.futures

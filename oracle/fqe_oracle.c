@@ -3,7 +3,8 @@
  *
  * A CPU restatement, in plain C99 + OpenMP, of the reference OpenFermion-FQE
  * natives that lie on the restricted H·psi path.  It is used
- *   - by tests/ as the checker of the CUDA library (never as the thing tested),
+ *   - by tests/ as the reference the CUDA library's results are compared with
+ *     (never as the thing tested),
  *   - by bench.py's `cpu_baseline` leg and `--impl reference` arm as the timed
  *     CPU implementation of the reference algorithm (same loop structure as the
  *     reference: per-target sparse accumulation for the same-spin terms and the

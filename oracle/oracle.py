@@ -30,7 +30,8 @@ reference keeps in Python:
 ``ozaki_model.py`` beside it models this project's tensor-core contraction
 arithmetic in numpy (no reference counterpart) for tests/test_ozaki_model.py.
 
-Used by tests/ (as the checker), by ``__graft_entry__.smoke`` and by
+Used by tests/ (the results of the CUDA library are compared with it), by
+``__graft_entry__.smoke`` and by
 bench.py's CPU legs.  Its parity with the reference is pinned by
 tests/test_oracle_pins.py.
 """
