@@ -16,6 +16,13 @@ rank runs an independent replica (the path does not shard); rank 0 prints.
 The second half of the metric, Davidson time to a 1e-6 residual with the
 learned vs the plain diagonal preconditioner, is the "davidson" object of the
 same line (default sector norb=12 (6a,6b); --davidson-norb, --no-davidson).
+
+  python bench.py --configs      the other single-GPU configurations (norb 8
+                                 apply and Taylor step; norb 14 FP64 vs
+                                 tensor-core error, Taylor, diagonal-Coulomb
+                                 evolve), one JSON object
+  python bench.py --norb 16 --precision ozaki --no-davidson
+                                 the 165.6 M-determinant sector
 """
 
 import argparse
