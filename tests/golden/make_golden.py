@@ -67,6 +67,32 @@ def graph_fixture():
     save("graphs", **out)
 
 
+def graph_pickles_fixture():
+    """The reference's own stored FciGraph objects
+    (tests/unittest_data/fci_graph/NNAANBNO.pickle, checked by
+    tests/fci_graph_test.py), unpacked into the tables of graph_fixture."""
+    import pickle
+    src = os.path.join(ref_fqe.REF_ROOT, "tests", "unittest_data", "fci_graph")
+    out = {}
+    for f in sorted(os.listdir(src)):
+        if not f.endswith(".pickle"):
+            continue
+        with open(os.path.join(src, f), "rb") as fh:
+            g = pickle.load(fh)["graph"]
+        norb, na, nb = g._norb, g._nalpha, g._nbeta
+        tag = f"{norb}_{na}_{nb}"
+        out[f"astr_{tag}"] = numpy.asarray(g._astr, dtype=numpy.uint64)
+        out[f"bstr_{tag}"] = numpy.asarray(g._bstr, dtype=numpy.uint64)
+        out[f"dexca_{tag}"] = numpy.asarray(g._dexca, dtype=numpy.int32)
+        out[f"dexcb_{tag}"] = numpy.asarray(g._dexcb, dtype=numpy.int32)
+        maps = [numpy.asarray(g._alpha_map[(i, j)], dtype=numpy.int32).reshape(-1, 3)
+                for i in range(norb) for j in range(norb)]
+        out[f"amaplen_{tag}"] = numpy.array([len(m) for m in maps], dtype=numpy.int32)
+        out[f"amaps_{tag}"] = (numpy.concatenate(maps) if maps else
+                               numpy.zeros((0, 3), numpy.int32))
+    save("graph_pickles", **out)
+
+
 def make_tensors(norb, kind, seed):
     rng = numpy.random.default_rng(1000 + seed)
     if kind == "real":
@@ -425,6 +451,6 @@ def chebyshev_fixture():
 if __name__ == "__main__":
     which = sys.argv[1:] or ["graph", "apply", "dc", "taylor", "dvec",
                              "davidson", "rdm", "rdm12", "spin", "wfn_pickles",
-                             "transform", "chebyshev"]
+                             "transform", "chebyshev", "graph_pickles"]
     for name in which:
         globals()[name + "_fixture"]()

@@ -38,6 +38,22 @@ def test_graph_tables_match_fixture(golden, oracle):
         numpy.testing.assert_array_equal(g.amaps, gd["amaps_" + tag])
 
 
+def test_graph_tables_match_reference_pickles(golden, oracle):
+    # the reference's own stored graphs (tests/unittest_data/fci_graph/*.pickle)
+    gd = golden("graph_pickles")
+    tags = [k[5:] for k in gd if k.startswith("astr_")]
+    assert len(tags) >= 4
+    for tag in tags:
+        norb, na, nb = map(int, tag.split("_"))
+        g = oracle.graph(norb, na, nb)
+        numpy.testing.assert_array_equal(g.astr, gd["astr_" + tag])
+        numpy.testing.assert_array_equal(g.bstr, gd["bstr_" + tag])
+        numpy.testing.assert_array_equal(g.dexca, gd["dexca_" + tag])
+        numpy.testing.assert_array_equal(g.dexcb, gd["dexcb_" + tag])
+        numpy.testing.assert_array_equal(g.alens.ravel(), gd["amaplen_" + tag])
+        numpy.testing.assert_array_equal(g.amaps, gd["amaps_" + tag])
+
+
 def test_string_order_known_answer(oracle):
     # tests/fci_graph_test.py:34-39 of the reference: the 70 strings of
     # (4 electrons, 8 orbitals) in address order begin 15, 23, 39, 71, 135 and
