@@ -370,3 +370,19 @@ def test_chebyshev_matches_fixture(golden, oracle):
         # applies twice (inside H and again at the end)
         e0, t = complex(gd["e0_" + tag]), float(gd["t_" + tag])
         assert abs(numpy.linalg.norm(out) - numpy.exp(2 * t * e0.imag)) < 1e-11
+
+
+def test_orbital_transform_is_a_representation(oracle):
+    # compound matrices compose (Cauchy-Binet: C(M1 M2) = C(M1) C(M2)) and a
+    # unitary orbital rotation keeps the sector's norm
+    from scipy.stats import unitary_group
+    norb, na, nb = 5, 2, 3
+    g = oracle.graph(norb, na, nb)
+    U1 = unitary_group.rvs(norb, random_state=7)
+    U2 = unitary_group.rvs(norb, random_state=8)
+    rng = numpy.random.default_rng(9)
+    psi = rng.normal(size=(g.lena, g.lenb)) + 1j * rng.normal(size=(g.lena, g.lenb))
+    both = oracle.transform_orbitals(psi, U1 @ U2, U1 @ U2, g)
+    step = oracle.transform_orbitals(oracle.transform_orbitals(psi, U2, U2, g), U1, U1, g)
+    assert numpy.abs(both - step).max() < 1e-12
+    assert abs(numpy.linalg.norm(both) - numpy.linalg.norm(psi)) < 1e-12
