@@ -271,7 +271,19 @@ def run_gpu(args):
               s3.ctypes.data_as(ctypes.c_void_p))
     stage[:] = s3
     _lib.call("fqegpu_ham_set_timing", ham.handle, 0)
+    # the applies are asynchronous: a tensor-core timeout would be reported here
+    _lib.call("fqegpu_ham_check", ham.handle, sptr)
     clocks = clk.summary()
+    # error of the timed result against the FP64 GPU apply (validated against
+    # the oracle by the tests), computed once outside the timed region
+    rel_err = None
+    if prec != "fp64":
+        sigma64 = torch.empty_like(sigma)
+        _lib.call("fqegpu_apply", ham.handle, _ptr(d.coeff), _ptr(sigma64),
+                  1.0, 0.0, 0.0, 0.0, _lib.PREC_FP64, sptr)
+        torch.cuda.synchronize()
+        rel_err = float(torch.linalg.norm(sigma - sigma64) / torch.linalg.norm(sigma64))
+        del sigma64
 
     t_max = max_over_ranks(ms, world)
     value = job_value(n, world, t_max / 1e3)
@@ -394,6 +406,7 @@ def run_gpu(args):
         "roofline": roofline,
         "stages": stages,
         "apply_hbm_view": apply_hbm,
+        "rel_err_vs_fp64": rel_err,
         "clocks": clocks,
         "cpu_baseline": cpu,
     }

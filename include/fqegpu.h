@@ -98,13 +98,17 @@ int fqegpu_graph_maps(fqegpu_graph g, int spin, int32_t *h_out);
  * symmetries, as fqe_data.py:658-681 does for real integrals. */
 int fqegpu_ham_create(fqegpu_graph g, const double *h_h1, const double *h_h2,
                       void *stream, fqegpu_ham *out);
+/* FQEGPU_ERR_INVALID (and nothing is freed) while a batch recorded with the
+ * handle exists: destroy the batch first. */
 int fqegpu_ham_destroy(fqegpu_ham h);
 /* info[0] = pair count P, info[1] = 1 if compressed, info[2] = 1 if the
  * integrals are a complex scalar times a real tensor, info[3] = scratch bytes
  * of one apply at the current block width. */
 int fqegpu_ham_info(fqegpu_ham h, int64_t *info4);
 /* Upper bound on device scratch one apply may hold (default: 40% of free
- * memory at creation).  Smaller limits stream narrower beta-column blocks. */
+ * memory at creation).  Smaller limits stream narrower beta-column blocks.
+ * Refused (FQEGPU_ERR_INVALID) while a batch recorded with the handle exists,
+ * since the batch's graph holds the current workspace. */
 int fqegpu_ham_set_scratch_limit(fqegpu_ham h, int64_t bytes);
 
 /* Per-stage device time of the last apply on this handle (milliseconds,
@@ -124,10 +128,20 @@ int fqegpu_ham_stage_ms(fqegpu_ham h, double *h_ms3);
  * (lib/fqe_data.c:668-720, :973-996; Cython wrappers _fqe_data.pyx:609-765),
  * and for one-body operators lm_apply_array1 (lib/fqe_data.c:272-302).
  * Wavefunction._apply_array's e_0 term (wavefunction.py:396-397) is beta.
- * d_psi and d_sigma must not alias. */
+ * d_psi and d_sigma must not alias.
+ * Asynchronous on `stream` for both precisions (no host synchronisation), so
+ * applies can be chained.  A bounded device wait of the tensor-core kernel
+ * that gives up sets a sticky error word of the handle; it is reported as
+ * FQEGPU_ERR_TIMEOUT by fqegpu_ham_check, or by a later apply on the handle
+ * once the failed apply has finished (that later apply then does nothing). */
 int fqegpu_apply(fqegpu_ham h, const double *d_psi, double *d_sigma,
                  double alpha_re, double alpha_im, double beta_re,
                  double beta_im, int precision, void *stream);
+/* Waits for `stream` and reports (then clears) the handle's sticky error
+ * word: FQEGPU_ERR_TIMEOUT when a tensor-core apply since the last check
+ * gave up a bounded wait.  The synchronous entry points (fqegpu_apply_host,
+ * fqegpu_taylor, fqegpu_batch_check) check by themselves. */
+int fqegpu_ham_check(fqegpu_ham h, void *stream);
 /* Same with host buffers: copies psi in and sigma out (pageable or pinned),
  * synchronous; the device staging buffer is allocated on the first call and
  * kept by the handle.  This is the call a ctypes binding inside the
@@ -205,7 +219,9 @@ int fqegpu_block_axpy(int64_t n, int k, const double *h_coef,
  * one uncaptured pass that allocates every workspace and tensor-core plan.
  * fqegpu_batch_launch replays the batch with one graph launch (asynchronous);
  * fqegpu_batch_check synchronises `stream` and reports a tensor-core timeout
- * of the last launch.  Buffers are those given at creation. */
+ * of the last launch.  Buffers are those given at creation.  While a batch
+ * exists its handles refuse fqegpu_ham_destroy and
+ * fqegpu_ham_set_scratch_limit (the graph holds their workspaces). */
 typedef struct fqegpu_batch_s *fqegpu_batch;
 int fqegpu_batch_create(int n, const fqegpu_ham *hams,
                         const double *const *d_psis, double *const *d_sigmas,
@@ -215,6 +231,22 @@ int fqegpu_batch_create(int n, const fqegpu_ham *hams,
 int fqegpu_batch_launch(fqegpu_batch b, void *stream);
 int fqegpu_batch_check(fqegpu_batch b, void *stream);
 int fqegpu_batch_destroy(fqegpu_batch b);
+/* Taylor series of many sectors in one CUDA graph: for every i,
+ *   d_psis[i] <- sum_k (-i t H_i)^k / k! d_psis[i]
+ * with each sector's own stopping test (||term|| < accuracy, at most
+ * expansion-1 orders; the device-resident loop of fqegpu_taylor), the sectors
+ * spread over parallel branches of the graph.  No e_0 phase.  hams must be
+ * distinct.  fqegpu_batch_launch runs one evolution of every sector (in
+ * place, asynchronous); fqegpu_batch_taylor_terms waits, writes the number of
+ * terms of each sector to h_terms[n] (may be NULL) and returns
+ * FQEGPU_ERR_NUMERIC if a series did not converge.  Reference:
+ * Wavefunction.apply_generated_unitary 'taylor' (wavefunction.py:553-568)
+ * applied sector by sector. */
+int fqegpu_batch_taylor_create(int n, const fqegpu_ham *hams,
+                               double *const *d_psis, double time,
+                               double accuracy, int expansion, int precision,
+                               void *stream, fqegpu_batch *out);
+int fqegpu_batch_taylor_terms(fqegpu_batch b, int *h_terms, void *stream);
 
 /* ---- one-particle RDM -------------------------------------------------------
  * h_rdm[i][j] = <bra| E_ij |ket>, E_ij = sum over spin of a+_i a_j, complex128
@@ -232,7 +264,12 @@ int fqegpu_rdm1(fqegpu_graph g, const double *d_bra, const double *d_ket,
  * Wavefunction.apply_generated_unitary 'taylor' (wavefunction.py:553-568,
  * 605-606) and time_evolve's two-body branch (wavefunction.py:1042-1045).
  * *h_terms receives the number of applies.  FQEGPU_ERR_NUMERIC if the series
- * does not reach the accuracy (the reference raises RuntimeError). */
+ * does not reach the accuracy (the reference raises RuntimeError) or a term's
+ * norm is not finite.  The series runs on the device as one CUDA graph (a
+ * conditional WHILE node whose body is one order: apply, accumulation, norm,
+ * stopping test); the host reads the loop state once, at the end.  The graph
+ * is kept by the handle and reused while the arguments stay the same.
+ * Synchronous. */
 int fqegpu_taylor(fqegpu_ham h, double *d_psi, double time, double e0_re,
                   double e0_im, double accuracy, int expansion, int precision,
                   int *h_terms, void *stream);
@@ -293,6 +330,19 @@ int fqegpu_mlp_loss_grad(fqegpu_mlp m, fqegpu_graph g, const double *d_u,
  * weights. */
 int fqegpu_mlp_adam(fqegpu_mlp m, double lr, double beta1, double beta2,
                     double eps, double grad_scale, void *stream);
+
+/* ---- test hooks (no counterpart in the reference) --------------------------
+ * Failure detection is tested without a GPU fault: the tensor-core kernel's
+ * bounded waits give up after `wait_cycles` clock cycles (<= 0: the default,
+ * about 2 s) and, with skip_slot >= 0, the loader of its first CTA leaves that
+ * ring slot of its first tile pair unfilled, so the consumer's wait runs out
+ * and the apply reports FQEGPU_ERR_TIMEOUT (the kernel waits for its issued
+ * copies and frees its tensor memory before it exits).  skip_slot = -1 and
+ * wait_cycles = 0 restore normal operation.  fqegpu_debug_fail_allocs makes
+ * the library's next `count` device allocations fail as on an exhausted
+ * device (FQEGPU_ERR_NOMEM). */
+int fqegpu_ham_test_injection(fqegpu_ham h, int64_t wait_cycles, int skip_slot);
+int fqegpu_debug_fail_allocs(int count);
 
 #ifdef __cplusplus
 }

@@ -273,15 +273,29 @@ static int ensure_workspace(fqegpu_ham h) {
   w = std::min<int64_t>(std::max<int64_t>(w, 1), lenb);
   const size_t bytes = (size_t)(per_col * w);
   if (h->d_ws && h->block_w == w) return FQEGPU_OK;
+  if (h->live_graphs > 0) {
+    set_error("the handle's workspace is held by %d recorded CUDA graph(s) and cannot be "
+              "reallocated; destroy them first", h->live_graphs);
+    return FQEGPU_ERR_INVALID;
+  }
   if (h->d_ws) {
     cudaFree(h->d_ws);
     h->d_ws = nullptr;
     h->ws_bytes = 0;
   }
-  FQE_CUDA(cudaMalloc(&h->d_ws, bytes));
+  FQE_CUDA(dev_alloc(&h->d_ws, bytes));
   h->ws_bytes = bytes;
   h->block_w = w;
   return FQEGPU_OK;
+}
+
+int apply_prepare(fqegpu_ham h, int precision) {
+  if (h->zero || h->onebody) return FQEGPU_OK;
+  if (precision == FQEGPU_PREC_OZAKI) {
+    const int s = ozaki_prepare(h);
+    if (s != FQEGPU_ERR_UNSUPPORTED) return s;
+  }
+  return ensure_workspace(h);
 }
 
 int apply_fp64(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
@@ -365,42 +379,40 @@ int stage_mark(fqegpu_ham h, int blk, int k, cudaStream_t st) {
 
 // ---------------------------------------------------------------------------
 // Host-side preparation of (h1, h2) (fqe_data.py:691-693 and the compressed
-// branch's symmetry assumption, fqe_data.py:658-681).
-static int prepare(fqegpu_ham h, const double* h_h1, const double* h_h2) {
-  const int n = h->norb;
+// branch's symmetry assumption, fqe_data.py:658-681); declared in ham.cuh.
+void prepare_pairs(int n, int nele, const zd* H1, const zd* H2, PairMatrix& out) {
   const int n2 = n * n;
-  const zd* H1 = (const zd*)h_h1;
-  const zd* H2 = (const zd*)h_h2;
-  h->h1p.assign((size_t)n2, zd(0.0, 0.0));
+  out = PairMatrix();
+  out.h1p.assign((size_t)n2, zd(0.0, 0.0));
   if (H1)
-    for (int k = 0; k < n2; ++k) h->h1p[k] = H1[k];
-  h->onebody = (H2 == nullptr);
-  if (!h->onebody) {
+    for (int k = 0; k < n2; ++k) out.h1p[k] = H1[k];
+  out.onebody = (H2 == nullptr);
+  if (!out.onebody) {
     // V'[ij][kl] = h2'[i,j,k,l] = -h2[i,k,j,l];  h1' = h1 + sum_k h2[i,k,k,j]
-    h->v2.assign((size_t)n2 * n2, zd(0.0, 0.0));
+    out.v2.assign((size_t)n2 * n2, zd(0.0, 0.0));
     for (int i = 0; i < n; ++i)
       for (int j = 0; j < n; ++j)
         for (int k = 0; k < n; ++k)
           for (int l = 0; l < n; ++l)
-            h->v2[(size_t)(i * n + j) * n2 + (k * n + l)] =
+            out.v2[(size_t)(i * n + j) * n2 + (k * n + l)] =
                 -H2[((size_t)(i * n + k) * n + j) * n + l];
     for (int i = 0; i < n; ++i)
       for (int j = 0; j < n; ++j) {
         zd s(0.0, 0.0);
         for (int k = 0; k < n; ++k) s += H2[((size_t)(i * n + k) * n + k) * n + j];
-        h->h1p[i * n + j] += s;
+        out.h1p[i * n + j] += s;
       }
   }
   // Full pair matrix (or one-body vector) in the uncompressed space.
   std::vector<zd> full;
-  if (h->onebody) {
-    full = h->h1p;
+  if (out.onebody) {
+    full = out.h1p;
   } else {
-    full = h->v2;
-    if (h->nele > 0) {
-      const double inv = 1.0 / (double)h->nele;
+    full = out.v2;
+    if (nele > 0) {
+      const double inv = 1.0 / (double)nele;
       for (int ij = 0; ij < n2; ++ij)
-        for (int k = 0; k < n; ++k) full[(size_t)ij * n2 + (k * n + k)] += h->h1p[ij] * inv;
+        for (int k = 0; k < n; ++k) full[(size_t)ij * n2 + (k * n + k)] += out.h1p[ij] * inv;
     }
   }
   double maxabs = 0.0;
@@ -412,11 +424,8 @@ static int prepare(fqegpu_ham h, const double* h_h1, const double* h_h2) {
       imax = k;
     }
   }
-  h->zero = (maxabs == 0.0) || h->nele == 0 || n == 0;
-  if (h->zero) {
-    h->P = 0;
-    return FQEGPU_OK;
-  }
+  out.zero = (maxabs == 0.0) || nele == 0 || n == 0;
+  if (out.zero) return;
   // Factor out a global phase; real if what remains has no imaginary part.
   zd ph = full[imax] / maxabs;
   if (ph.real() == 0.0 || ph.imag() == 0.0) ph = zd(ph.real() == 0.0 ? 0.0 : (ph.real() > 0 ? 1.0 : -1.0),
@@ -428,12 +437,12 @@ static int prepare(fqegpu_ham h, const double* h_h1, const double* h_h2) {
     rot[k] = full[k] * std::conj(ph);
     if (std::abs(rot[k].imag()) > tol) real = false;
   }
-  h->real = real;
-  h->phase = real ? make_double2(ph.real(), ph.imag()) : make_double2(1.0, 0.0);
+  out.real = real;
+  out.phase = real ? make_double2(ph.real(), ph.imag()) : make_double2(1.0, 0.0);
   const std::vector<zd>& src = real ? rot : full;
   // Compressible: symmetric under i<->j (and k<->l for the pair matrix).
   bool sym = true;
-  if (h->onebody) {
+  if (out.onebody) {
     for (int i = 0; i < n && sym; ++i)
       for (int j = 0; j < i && sym; ++j)
         if (std::abs(src[i * n + j] - src[j * n + i]) > tol) sym = false;
@@ -450,9 +459,9 @@ static int prepare(fqegpu_ham h, const double* h_h1, const double* h_h2) {
             }
           }
   }
-  h->compressed = sym;
+  out.compressed = sym;
   const int P = sym ? n * (n + 1) / 2 : n2;
-  h->P = P;
+  out.P = P;
   auto pair_of = [&](int p, int& i, int& j) {
     if (!sym) {
       i = p / n;
@@ -464,27 +473,18 @@ static int prepare(fqegpu_ham h, const double* h_h1, const double* h_h2) {
     i = a;
     j = p - a * (a + 1) / 2;
   };
-  if (h->onebody) {
-    std::vector<double> wr(P);
-    std::vector<double2> wc(P);
+  if (out.onebody) {
+    if (real) out.vr.resize(P); else out.vc.resize(P);
     for (int p = 0; p < P; ++p) {
       int i, j;
       pair_of(p, i, j);
       const zd v = src[i * n + j];
-      wr[p] = v.real();
-      wc[p] = make_double2(v.real(), v.imag());
+      if (real) out.vr[p] = v.real();
+      else out.vc[p] = make_double2(v.real(), v.imag());
     }
-    if (real) {
-      FQE_CUDA(cudaMalloc(&h->d_h1r, sizeof(double) * P));
-      FQE_CUDA(cudaMemcpy(h->d_h1r, wr.data(), sizeof(double) * P, cudaMemcpyHostToDevice));
-    } else {
-      FQE_CUDA(cudaMalloc(&h->d_h1c, sizeof(double2) * P));
-      FQE_CUDA(cudaMemcpy(h->d_h1c, wc.data(), sizeof(double2) * P, cudaMemcpyHostToDevice));
-    }
-    return FQEGPU_OK;
+    return;
   }
-  std::vector<double> vr((size_t)P * P);
-  std::vector<double2> vc((size_t)P * P);
+  if (real) out.vr.resize((size_t)P * P); else out.vc.resize((size_t)P * P);
   for (int p = 0; p < P; ++p) {
     int i, j;
     pair_of(p, i, j);
@@ -492,23 +492,52 @@ static int prepare(fqegpu_ham h, const double* h_h1, const double* h_h2) {
       int k, l;
       pair_of(q, k, l);
       const zd v = src[(size_t)(i * n + j) * n2 + k * n + l];
-      vr[(size_t)p * P + q] = v.real();
-      vc[(size_t)p * P + q] = make_double2(v.real(), v.imag());
+      if (real) out.vr[(size_t)p * P + q] = v.real();
+      else out.vc[(size_t)p * P + q] = make_double2(v.real(), v.imag());
     }
   }
-  if (real) {
-    h->vpair = vr;
-    FQE_CUDA(cudaMalloc(&h->d_Vr, sizeof(double) * P * P));
-    FQE_CUDA(cudaMemcpy(h->d_Vr, vr.data(), sizeof(double) * P * P, cudaMemcpyHostToDevice));
+}
+
+static int prepare(fqegpu_ham h, const double* h_h1, const double* h_h2) {
+  PairMatrix pm;
+  prepare_pairs(h->norb, h->nele, (const zd*)h_h1, (const zd*)h_h2, pm);
+  h->h1p = std::move(pm.h1p);
+  h->v2 = std::move(pm.v2);
+  h->onebody = pm.onebody;
+  h->zero = pm.zero;
+  if (h->zero) {
+    h->P = 0;
+    return FQEGPU_OK;
+  }
+  h->real = pm.real;
+  h->phase = pm.phase;
+  h->compressed = pm.compressed;
+  const int P = pm.P;
+  h->P = P;
+  if (h->onebody) {
+    if (pm.real) {
+      FQE_CUDA(dev_alloc(&h->d_h1r, sizeof(double) * P));
+      FQE_CUDA(cudaMemcpy(h->d_h1r, pm.vr.data(), sizeof(double) * P, cudaMemcpyHostToDevice));
+    } else {
+      FQE_CUDA(dev_alloc(&h->d_h1c, sizeof(double2) * P));
+      FQE_CUDA(cudaMemcpy(h->d_h1c, pm.vc.data(), sizeof(double2) * P, cudaMemcpyHostToDevice));
+    }
+    return FQEGPU_OK;
+  }
+  if (pm.real) {
+    FQE_CUDA(dev_alloc(&h->d_Vr, sizeof(double) * P * P));
+    FQE_CUDA(cudaMemcpy(h->d_Vr, pm.vr.data(), sizeof(double) * P * P, cudaMemcpyHostToDevice));
+    h->vpair = std::move(pm.vr);
   } else {
-    FQE_CUDA(cudaMalloc(&h->d_Vc, sizeof(double2) * P * P));
-    FQE_CUDA(cudaMemcpy(h->d_Vc, vc.data(), sizeof(double2) * P * P, cudaMemcpyHostToDevice));
+    FQE_CUDA(dev_alloc(&h->d_Vc, sizeof(double2) * P * P));
+    FQE_CUDA(cudaMemcpy(h->d_Vc, pm.vc.data(), sizeof(double2) * P * P, cudaMemcpyHostToDevice));
   }
   return FQEGPU_OK;
 }
 
 static void ham_free(fqegpu_ham h) {
   if (!h) return;
+  taylor_destroy(h);
   ozaki_destroy(h);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   cudaFree(h->d_Vr);
@@ -552,6 +581,12 @@ extern "C" int fqegpu_ham_create(fqegpu_graph g, const double* h_h1,
 }
 
 extern "C" int fqegpu_ham_destroy(fqegpu_ham h) {
+  clear_error();
+  if (h && h->live_graphs > 0) {
+    set_error("handle is held by %d recorded CUDA graph(s); destroy them first",
+              h->live_graphs);
+    return FQEGPU_ERR_INVALID;
+  }
   ham_free(h);
   return FQEGPU_OK;
 }
@@ -569,6 +604,8 @@ extern "C" int fqegpu_ham_info(fqegpu_ham h, int64_t* info4) {
 extern "C" int fqegpu_ham_set_scratch_limit(fqegpu_ham h, int64_t bytes) {
   clear_error();
   FQE_CHECK_ARG(h && bytes > 0, "bad arguments");
+  FQE_CHECK_ARG(h->live_graphs == 0,
+                "the handle is held by a recorded CUDA graph (batch); destroy it first");
   h->scratch_limit = bytes;
   return FQEGPU_OK;
 }
@@ -600,7 +637,7 @@ extern "C" int fqegpu_apply_host(fqegpu_ham h, const double* h_psi,
   // device staging: the handle's two-vector work buffer (also the Taylor
   // workspace), allocated once and kept, so a call costs the two copies and
   // the apply
-  if (!h->d_vec) FQE_CUDA(cudaMalloc(&h->d_vec, sizeof(double2) * 2 * (size_t)N));
+  if (!h->d_vec) FQE_CUDA(dev_alloc(&h->d_vec, sizeof(double2) * 2 * (size_t)N));
   double2* d = h->d_vec;
   int s = FQEGPU_OK;
   cudaError_t e = cudaMemcpy(d, h_psi, sizeof(double2) * N, cudaMemcpyHostToDevice);
@@ -614,7 +651,23 @@ extern "C" int fqegpu_apply_host(fqegpu_ham h, const double* h_psi,
     set_error("apply_host: %s", cudaGetErrorString(e));
     return FQEGPU_ERR_CUDA;
   }
+  if (s == FQEGPU_OK && h->oz) s = ozaki_check(h, nullptr);  // synchronous call: report now
   return s;
+}
+
+extern "C" int fqegpu_ham_check(fqegpu_ham h, void* stream) {
+  clear_error();
+  FQE_CHECK_ARG(h != nullptr, "NULL handle");
+  FQE_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  if (h->oz) return ozaki_check(h, (cudaStream_t)stream);
+  return FQEGPU_OK;
+}
+
+extern "C" int fqegpu_ham_test_injection(fqegpu_ham h, int64_t wait_cycles, int skip_slot) {
+  clear_error();
+  FQE_CHECK_ARG(h != nullptr, "NULL handle");
+  FQE_CHECK_ARG(skip_slot >= -1, "skip_slot must be >= -1");
+  return ozaki_set_test_injection(h, (long long)wait_cycles, skip_slot);
 }
 
 extern "C" int fqegpu_make_dvec(fqegpu_graph g, const double* d_psi,

@@ -43,6 +43,15 @@ void clear_error();
 
 constexpr int kNumSMs = 152;
 
+// Every device allocation of the library goes through dev_alloc, so a test
+// can make the next n of them fail as an exhausted device would
+// (fqegpu_debug_fail_allocs); otherwise it is cudaMalloc.
+cudaError_t dev_alloc_bytes(void** p, size_t bytes);
+template <class T>
+inline cudaError_t dev_alloc(T** p, size_t bytes) {
+  return dev_alloc_bytes(reinterpret_cast<void**>(p), bytes);
+}
+
 inline int64_t binom_host(int n, int k) {
   if (k < 0 || n < 0 || k > n) return 0;
   if (k > n - k) k = n - k;

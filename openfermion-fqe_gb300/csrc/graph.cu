@@ -199,11 +199,11 @@ static int build_spin(int norb, int nele, cudaStream_t st, SpinTables& t) {
   t.ndexc = nele * (norb - nele + 1);
   const int64_t len = t.len;
   const int P = norb * norb, PT = norb * (norb + 1) / 2;
-  FQE_CUDA(cudaMalloc(&t.strings, sizeof(uint64_t) * len));
-  FQE_CUDA(cudaMalloc(&t.zmat, sizeof(int32_t) * (size_t)(nele * norb > 0 ? nele * norb : 1)));
-  FQE_CUDA(cudaMalloc(&t.dexc, sizeof(int32_t) * 3 * (size_t)(len * t.ndexc > 0 ? len * t.ndexc : 1)));
-  FQE_CUDA(cudaMalloc(&t.tab_full, sizeof(int32_t) * (size_t)(P > 0 ? P : 1) * len));
-  FQE_CUDA(cudaMalloc(&t.tab_tri, sizeof(int32_t) * (size_t)(PT > 0 ? PT : 1) * len));
+  FQE_CUDA(dev_alloc(&t.strings, sizeof(uint64_t) * len));
+  FQE_CUDA(dev_alloc(&t.zmat, sizeof(int32_t) * (size_t)(nele * norb > 0 ? nele * norb : 1)));
+  FQE_CUDA(dev_alloc(&t.dexc, sizeof(int32_t) * 3 * (size_t)(len * t.ndexc > 0 ? len * t.ndexc : 1)));
+  FQE_CUDA(dev_alloc(&t.tab_full, sizeof(int32_t) * (size_t)(P > 0 ? P : 1) * len));
+  FQE_CUDA(dev_alloc(&t.tab_tri, sizeof(int32_t) * (size_t)(PT > 0 ? PT : 1) * len));
   FQE_CUDA(cudaMemsetAsync(t.tab_full, 0, sizeof(int32_t) * (size_t)(P > 0 ? P : 1) * len, st));
   FQE_CUDA(cudaMemsetAsync(t.tab_tri, 0, sizeof(int32_t) * (size_t)(PT > 0 ? PT : 1) * len, st));
   if (nele * norb > 0) {
@@ -349,8 +349,8 @@ extern "C" int fqegpu_graph_maps(fqegpu_graph g, int spin, int32_t* h_out) {
   if (total == 0) return FQEGPU_OK;
   int64_t* d_off = nullptr;
   int32_t* d_maps = nullptr;
-  FQE_CUDA(cudaMalloc(&d_off, sizeof(int64_t) * off.size()));
-  cudaError_t e = cudaMalloc(&d_maps, sizeof(int32_t) * 3 * total);
+  FQE_CUDA(dev_alloc(&d_off, sizeof(int64_t) * off.size()));
+  cudaError_t e = dev_alloc(&d_maps, sizeof(int32_t) * 3 * total);
   if (e == cudaSuccess)
     e = cudaMemcpy(d_off, off.data(), sizeof(int64_t) * off.size(),
                    cudaMemcpyHostToDevice);

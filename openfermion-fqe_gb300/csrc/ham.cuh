@@ -11,7 +11,31 @@ namespace fqegpu {
 
 using zd = std::complex<double>;
 
-struct OzakiPlan;  // tensor-core contraction state (ozaki.cu)
+struct OzakiPlan;    // tensor-core contraction state (ozaki.cu)
+struct TaylorGraph;  // recorded Taylor series of a handle (taylor.cu)
+
+// Host preparation of (h1, h2) for one sector (fqe_data.py:691-693 and the
+// compressed branch's symmetry assumption, fqe_data.py:658-681):
+//   V[ij][kl] = h2'[i,j,k,l] = -h2[i,k,j,l],  h1' = h1 + sum_k h2[i,k,k,j],
+// with the one-body part folded in as h1'[ij] delta_kl / N_e (two-body) or
+// kept as the weight vector h1' (one-body, h2 == NULL).  A global phase is
+// factored out when what remains is real (to 64 ulp of the largest entry);
+// the pair space is compressed to p = tri(i, j) when the tensors have the
+// real-orbital pair symmetries.  Used by fqegpu_ham_create and
+// fqegpu_apply_noalloc, so both apply the same operator.
+struct PairMatrix {
+  bool zero = false;        // identically zero on this sector
+  bool onebody = false;     // h2 == NULL
+  bool real = false;        // phase * (real tensor)
+  bool compressed = false;  // pair space p = tri(i, j)
+  double2 phase{1.0, 0.0};
+  int P = 0;
+  std::vector<zd> h1p;        // [norb][norb] prepared one-body h1'
+  std::vector<zd> v2;         // [norb^2][norb^2] prepared two-body V' (two-body only)
+  std::vector<double> vr;     // [P][P] (two-body) or [P] (one-body), real case
+  std::vector<double2> vc;    // same, complex case
+};
+void prepare_pairs(int norb, int nele, const zd* H1, const zd* H2, PairMatrix& out);
 
 int axpy_async(int64_t n, double2 a, const double2* x, double2* y, cudaStream_t st);
 int scale_async(int64_t n, double2 a, double2* x, cudaStream_t st);
@@ -49,6 +73,7 @@ struct fqegpu_ham_s {
   double2* d_vec = nullptr;  // 2 * N complex
   double2* d_red = nullptr;
   fqegpu::OzakiPlan* oz = nullptr;
+  fqegpu::TaylorGraph* taylor = nullptr;
   // Optional per-stage timing: 4 events per beta block (start, after gather,
   // after contraction, after scatter), recorded on the launching stream.
   bool timing = false;
@@ -57,6 +82,10 @@ struct fqegpu_ham_s {
   // Set while an apply is recorded into a CUDA graph: the tensor-core path
   // then skips its end-of-apply error readback (fqegpu_batch_check reads it).
   bool defer_check = false;
+  // Number of live CUDA graphs (batches, Taylor graphs) that hold this
+  // handle's workspace and plan pointers; while nonzero the handle refuses to
+  // reallocate them (scratch-limit changes) and to be destroyed.
+  int live_graphs = 0;
 };
 
 namespace fqegpu {
@@ -70,8 +99,33 @@ int apply_fp64(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
 int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
                 double2 beta, cudaStream_t st);
 void ozaki_destroy(fqegpu_ham h);
-// Error word of the tensor-core path's last apply (0 when none ran or OK).
-int ozaki_error_flag(fqegpu_ham h, int32_t* out);
+// Creates the tensor-core plan if the operator fits it (FQEGPU_ERR_UNSUPPORTED
+// otherwise: the apply then runs the FP64 kernels).
+int ozaki_prepare(fqegpu_ham h);
+// Waits for `st` and reports (and clears) the tensor-core path's sticky
+// error word: FQEGPU_ERR_TIMEOUT when a bounded wait gave up since the last
+// check.
+int ozaki_check(fqegpu_ham h, cudaStream_t st);
+// Test-only: wait limit of the tensor-core kernel (cycles; <= 0: default) and
+// a ring slot of CTA 0's first tile pair left unfilled (-1: none).
+int ozaki_set_test_injection(fqegpu_ham h, long long wait_cycles, int skip_slot);
+// Allocates what an apply of `precision` needs (plan, workspace) without
+// running it, so that the apply can be recorded into a CUDA graph.
+int apply_prepare(fqegpu_ham h, int precision);
+// Device-resident Taylor series (taylor.cu): bytes of one series' device
+// state; recording of one series of `h` on `psi` into the graph being
+// captured on `cs`, its loop body captured on `bs` (a stream that is not
+// capturing; uses h->d_vec, which must hold 2 N elements); reading of
+// a finished series' state (copied to the host) into the reference's
+// errors; the e_0 phase.
+size_t taylor_state_bytes();
+int taylor_record(fqegpu_ham h, double2* psi, double time, double accuracy, int expansion,
+                  int precision, void* state, cudaStream_t cs, cudaStream_t bs);
+int taylor_result(const void* h_state, int expansion, int* h_terms);
+int taylor_phase(double2* psi, int64_t N, double time, double e0_re, double e0_im,
+                 cudaStream_t st);
+void taylor_destroy(fqegpu_ham h);
+constexpr size_t kTaylorStateHostBytes = 32;  // sizeof(TaylorState)
 // Gather / scatter building blocks (apply.cu).
 int launch_gather(const fqegpu_graph_s* g, bool tri, int P, int64_t c0,
                   int64_t w, const double2* psi, double2* D, cudaStream_t st);

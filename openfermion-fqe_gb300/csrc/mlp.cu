@@ -452,14 +452,14 @@ int fqegpu_mlp_create(fqegpu_mlp* out) {
   auto* m = new fqegpu_mlp_s();
   m->fwd_blocks = kNumSMs * 8;
   cudaError_t e = cudaSuccess;
-  e = e ? e : cudaMalloc(&m->master, kParams * sizeof(float));
-  e = e ? e : cudaMalloc(&m->wbf, kParams * sizeof(__nv_bfloat16));
-  e = e ? e : cudaMalloc(&m->m1, kParams * sizeof(float));
-  e = e ? e : cudaMalloc(&m->m2, kParams * sizeof(float));
-  e = e ? e : cudaMalloc(&m->grad, kParams * sizeof(float));
-  e = e ? e : cudaMalloc(&m->gpart, (size_t)kBwdBlocks * kParams * sizeof(float));
-  e = e ? e : cudaMalloc(&m->part, (size_t)m->fwd_blocks * kRed * sizeof(double));
-  e = e ? e : cudaMalloc(&m->scal, 16 * sizeof(double));
+  e = e ? e : dev_alloc(&m->master, kParams * sizeof(float));
+  e = e ? e : dev_alloc(&m->wbf, kParams * sizeof(__nv_bfloat16));
+  e = e ? e : dev_alloc(&m->m1, kParams * sizeof(float));
+  e = e ? e : dev_alloc(&m->m2, kParams * sizeof(float));
+  e = e ? e : dev_alloc(&m->grad, kParams * sizeof(float));
+  e = e ? e : dev_alloc(&m->gpart, (size_t)kBwdBlocks * kParams * sizeof(float));
+  e = e ? e : dev_alloc(&m->part, (size_t)m->fwd_blocks * kRed * sizeof(double));
+  e = e ? e : dev_alloc(&m->scal, 16 * sizeof(double));
   e = e ? e : cudaMemset(m->master, 0, kParams * sizeof(float));
   e = e ? e : cudaMemset(m->wbf, 0, kParams * sizeof(__nv_bfloat16));
   e = e ? e : cudaMemset(m->m1, 0, kParams * sizeof(float));

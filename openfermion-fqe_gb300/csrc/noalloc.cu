@@ -61,99 +61,6 @@ int scratch_address(unsigned char** out) {
 
 size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// Host preparation of the pair matrix, the same rules as fqegpu_ham_create:
-// V[ij][kl] = -h2[i,k,j,l] + h1'[ij] delta_kl / N_e, h1' = h1 + sum_k
-// h2[i,k,k,j]; a global phase is factored out when what remains is real, and
-// the pair space is compressed when V has the real-orbital pair symmetries.
-struct HostPairs {
-  bool zero = false, real = false, compressed = false;
-  double2 phase{1.0, 0.0};
-  int P = 0;
-  std::vector<double> vr;
-  std::vector<double2> vc;
-};
-
-void prepare_pairs(int n, int nele, const zd* H1, const zd* H2, HostPairs& out) {
-  const int n2 = n * n;
-  std::vector<zd> h1p((size_t)n2, zd(0.0, 0.0)), full((size_t)n2 * n2);
-  if (H1)
-    for (int k = 0; k < n2; ++k) h1p[k] = H1[k];
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) {
-      zd s(0.0, 0.0);
-      for (int k = 0; k < n; ++k) s += H2[((size_t)(i * n + k) * n + k) * n + j];
-      h1p[i * n + j] += s;
-    }
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j)
-      for (int k = 0; k < n; ++k)
-        for (int l = 0; l < n; ++l)
-          full[(size_t)(i * n + j) * n2 + (k * n + l)] = -H2[((size_t)(i * n + k) * n + j) * n + l];
-  if (nele > 0)
-    for (int ij = 0; ij < n2; ++ij)
-      for (int k = 0; k < n; ++k) full[(size_t)ij * n2 + (k * n + k)] += h1p[ij] / (double)nele;
-  double maxabs = 0.0;
-  size_t imax = 0;
-  for (size_t k = 0; k < full.size(); ++k)
-    if (std::abs(full[k]) > maxabs) {
-      maxabs = std::abs(full[k]);
-      imax = k;
-    }
-  out.zero = maxabs == 0.0 || nele == 0 || n == 0;
-  if (out.zero) return;
-  zd ph = full[imax] / maxabs;
-  if (ph.real() == 0.0 || ph.imag() == 0.0)
-    ph = zd(ph.real() == 0.0 ? 0.0 : (ph.real() > 0 ? 1.0 : -1.0),
-            ph.imag() == 0.0 ? 0.0 : (ph.imag() > 0 ? 1.0 : -1.0));
-  const double tol = 64.0 * DBL_EPSILON * maxabs;
-  std::vector<zd> rot(full.size());
-  bool real = true;
-  for (size_t k = 0; k < full.size(); ++k) {
-    rot[k] = full[k] * std::conj(ph);
-    if (std::abs(rot[k].imag()) > tol) real = false;
-  }
-  out.real = real;
-  out.phase = real ? make_double2(ph.real(), ph.imag()) : make_double2(1.0, 0.0);
-  const std::vector<zd>& src = real ? rot : full;
-  bool sym = true;
-  for (int i = 0; i < n && sym; ++i)
-    for (int j = 0; j < n && sym; ++j)
-      for (int k = 0; k < n && sym; ++k)
-        for (int l = 0; l < n; ++l) {
-          const zd v = src[(size_t)(i * n + j) * n2 + k * n + l];
-          if (std::abs(v - src[(size_t)(j * n + i) * n2 + k * n + l]) > tol ||
-              std::abs(v - src[(size_t)(i * n + j) * n2 + l * n + k]) > tol) {
-            sym = false;
-            break;
-          }
-        }
-  out.compressed = sym;
-  const int P = sym ? n * (n + 1) / 2 : n2;
-  out.P = P;
-  auto pair_of = [&](int p, int& i, int& j) {
-    if (!sym) {
-      i = p / n;
-      j = p % n;
-      return;
-    }
-    int a = 0;
-    while ((a + 1) * (a + 2) / 2 <= p) ++a;
-    i = a;
-    j = p - a * (a + 1) / 2;
-  };
-  if (real) out.vr.resize((size_t)P * P); else out.vc.resize((size_t)P * P);
-  for (int p = 0; p < P; ++p) {
-    int i, j;
-    pair_of(p, i, j);
-    for (int q = 0; q < P; ++q) {
-      int k, l;
-      pair_of(q, k, l);
-      const zd v = src[(size_t)(i * n + j) * n2 + k * n + l];
-      if (real) out.vr[(size_t)p * P + q] = v.real();
-      else out.vc[(size_t)p * P + q] = make_double2(v.real(), v.imag());
-    }
-  }
-}
 }  // namespace
 }  // namespace fqegpu
 
@@ -181,10 +88,15 @@ extern "C" int fqegpu_apply_noalloc(int norb, int nalpha, int nbeta, const doubl
     return FQEGPU_ERR_UNSUPPORTED;
   }
 
-  HostPairs hp;
+  // the same pair matrix fqegpu_ham_create prepares (ham.cuh: prepare_pairs)
+  PairMatrix hp;
   prepare_pairs(norb, nalpha + nbeta, reinterpret_cast<const zd*>(h_h1),
                 reinterpret_cast<const zd*>(h_h2), hp);
-  if (hp.zero) return launch_axpby(N, beta, psi, sigma, st);
+  if (hp.zero) {
+    FQE_TRY(launch_axpby(N, beta, psi, sigma, st));
+    FQE_CUDA(cudaStreamSynchronize(st));  // synchronous on every path
+    return FQEGPU_OK;
+  }
 
   unsigned char* base = nullptr;
   FQE_TRY(scratch_address(&base));

@@ -43,6 +43,7 @@
 // Every wait in k_oz_mma is bounded; on a timeout the kernel records an
 // error, lets the other roles leave, and frees its TMEM.
 #include <cuda_bf16.h>
+#include <math_constants.h>
 
 #include <algorithm>
 #include <cmath>
@@ -72,8 +73,9 @@ constexpr int kLoadWarp = 17;
 constexpr int kThreads = 18 * 32;
 constexpr int kAccs = 4;           // levels 2, 3, 4 and 5..7
 constexpr uint32_t kTmemCols = kAccs * kNM;  // 512: one accumulator set
-constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
+constexpr long long kWaitCycles = 4000000000ll;  // default wait limit: ~2 s at 2 GHz
 constexpr int kExpZero = -2000;
+constexpr int kExpNonFinite = 30000;  // row exponent of a row holding Inf or NaN
 }  // namespace
 
 struct OzakiPlan {
@@ -98,6 +100,18 @@ struct OzakiPlan {
   int ring = 0;
   int nsm = 0;
   size_t smem = 0;
+  // error reporting without a host synchronisation per apply: d_misc[1] is
+  // a sticky error word (set by a kernel whose bounded wait gave up, cleared
+  // only by a check); after each apply it is copied to pinned h_err and
+  // err_ev recorded, so the next apply can poll it without blocking
+  int32_t* h_err = nullptr;
+  cudaEvent_t err_ev = nullptr;
+  bool err_pending = false;
+  // bounded-wait limit (clock cycles) and a test-only fault injection: when
+  // skip_slot >= 0 the loader of CTA 0 leaves that ring slot of its first
+  // tile pair unfilled, so the MMA warp's wait on it must run out
+  long long wait_cycles = kWaitCycles;
+  int skip_slot = -1;
 };
 
 struct OzArgs {
@@ -118,6 +132,8 @@ struct OzArgs {
   __nv_bfloat16* dslices;  // [ntiles][5][64 * KP]
   float4* G;
   int32_t* err;
+  long long wait_cycles;  // limit of every bounded wait
+  int skip_slot;          // test-only: slot of CTA 0's first tile pair left unfilled (-1: none)
 };
 
 // Tile t -> (alpha row, first beta column).  Tiles are visited in column
@@ -136,15 +152,25 @@ __device__ __forceinline__ void tile_coords(const OzArgs& A, int64_t t, int64_t&
 
 // Bounded wait that also gives up when another role has aborted.
 __device__ __forceinline__ bool oz_wait(uint64_t* bar, uint32_t parity,
-                                        volatile int* abort_flag) {
+                                        volatile int* abort_flag, long long limit) {
   if (tc::mbar_try_wait(bar, parity)) return true;  // fast path: no clock read
   const long long t0 = clock64();
   for (uint32_t it = 0;; ++it) {
     if (tc::mbar_try_wait(bar, parity)) return true;
     if ((it & 255u) == 255u) {
       if (*abort_flag) return false;
-      if (clock64() - t0 > kWaitCycles) return false;
+      if (clock64() - t0 > limit) return false;
     }
+  }
+}
+
+// Bounded wait that ignores the abort flag: for copies already issued, which
+// complete on their own (they depend on nothing but global memory).
+__device__ __forceinline__ bool oz_wait_drain(uint64_t* bar, uint32_t parity, long long limit) {
+  const long long t0 = clock64();
+  for (uint32_t it = 0;; ++it) {
+    if (tc::mbar_try_wait(bar, parity)) return true;
+    if ((it & 255u) == 255u && clock64() - t0 > limit) return false;
   }
 }
 
@@ -404,29 +430,55 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       // ring position and phase advance incrementally (no 64-bit division)
       int slot = 0;
       uint32_t ph = 0;
-      for (int64_t t = t_begin; t < t_end; ++t) {
+      int64_t issued = 0;      // slots filled (or, once, deliberately skipped)
+      int skipped = -1;        // ring index of the skipped fill (test injection)
+      uint32_t skipped_ph = 0;
+      bool ok = true;
+      for (int64_t t = t_begin; t < t_end && ok; ++t) {
         const __nv_bfloat16* src =
             A.dslices + (size_t)t * kSlices * nch * kPairChunkElems;
-        bool ok = true;
         for (int b = 0; b < kSlices && ok; ++b) {
           for (int gi = 0; gi < ngr; ++gi) {
             const int c0 = gi * kGroupK;
             const uint32_t bytes = (uint32_t)min(kGroupK, nch - c0) * pchunk_bytes;
-            if (!oz_wait(&empty[slot], ph ^ 1u, abort_flag)) {
+            if (!oz_wait(&empty[slot], ph ^ 1u, abort_flag, A.wait_cycles)) {
               oz_abort(abort_flag, A.err, 5);
               ok = false;
               break;
             }
-            tc::mbar_arrive_expect_tx(&full[slot], bytes);
-            tc::bulk_g2s(sD + (size_t)slot * slot_elems,
-                         src + ((size_t)b * nch + c0) * kPairChunkElems, bytes, &full[slot]);
+            const bool skip = A.skip_slot >= 0 && blockIdx.x == 0 && t == t_begin &&
+                              issued == A.skip_slot;
+            if (skip) {
+              // test injection: neither arrive nor copy, so the consumer's
+              // bounded wait on this slot runs out
+              skipped = slot;
+              skipped_ph = ph;
+            } else {
+              tc::mbar_arrive_expect_tx(&full[slot], bytes);
+              tc::bulk_g2s(sD + (size_t)slot * slot_elems,
+                           src + ((size_t)b * nch + c0) * kPairChunkElems, bytes, &full[slot]);
+            }
+            ++issued;
             if (++slot == R) {
               slot = 0;
               ph ^= 1u;
             }
           }
         }
-        if (!ok) break;
+      }
+      // Before the CTA may exit, every bulk copy issued into shared memory
+      // must have landed: wait for the last fill of each slot (on the normal
+      // path the MMA warp has already consumed them all).
+      const int64_t nlast = issued < R ? issued : R;
+      int s2 = slot;
+      uint32_t p2 = ph;
+      for (int64_t k = 0; k < nlast; ++k) {
+        if (--s2 < 0) {
+          s2 = R - 1;
+          p2 ^= 1u;
+        }
+        if (s2 == skipped && p2 == skipped_ph) continue;
+        if (!oz_wait_drain(&full[s2], p2, A.wait_cycles + kWaitCycles)) oz_abort(abort_flag, A.err, 7);
       }
     }
   } else if (warp == kMmaWarp) {
@@ -453,7 +505,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
     bool ok = true;
     for (int64_t t = t_begin; t < t_end && ok; ++t, ++it) {
       // warp-uniform outcome of every wait
-      if (!__all_sync(0xffffffffu, oz_wait(accempty, (uint32_t)((it & 1) ^ 1), abort_flag))) {
+      if (!__all_sync(0xffffffffu,
+                      oz_wait(accempty, (uint32_t)((it & 1) ^ 1), abort_flag, A.wait_cycles))) {
         if (elect) oz_abort(abort_flag, A.err, 2);
         ok = false;
         break;
@@ -466,7 +519,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
         for (int gi = 0; gi < ngr && ok; ++gi) {
           const int c0 = gi * kGroupK;
           const int nk = min(kGroupK, nch - c0);
-          if (!__all_sync(0xffffffffu, oz_wait(&full[slot], ph, abort_flag))) {
+          if (!__all_sync(0xffffffffu, oz_wait(&full[slot], ph, abort_flag, A.wait_cycles))) {
             if (elect) oz_abort(abort_flag, A.err, 3);
             ok = false;
             break;
@@ -511,7 +564,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
     // every MMA issued above has completed before TMEM is released
     if (elect) {
       tc::mma_commit(done);
-      if (!oz_wait(done, 0, abort_flag) && !*abort_flag) oz_abort(abort_flag, A.err, 6);
+      // MMAs always complete: this wait ignores the abort flag
+      if (!oz_wait_drain(done, 0, A.wait_cycles + kWaitCycles)) oz_abort(abort_flag, A.err, 6);
     }
     __syncwarp();
   } else {
@@ -537,7 +591,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
         bits = part ? be.y : be.x;
       }
       const bool got = __all_sync(0xffffffffu,
-                                  oz_wait(accfull, (uint32_t)(it & 1), abort_flag));
+                                  oz_wait(accfull, (uint32_t)(it & 1), abort_flag, A.wait_cycles));
       if (!got) {
         if (lane == 0) oz_abort(abort_flag, A.err, 4);
         break;
@@ -608,9 +662,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
 
 // ---- pre-pass: global exponent and the fixed-point copy of psi ------------
 __device__ __forceinline__ int exp_of(double x) {
-  // e with |x| < 2^e (frexp convention); kExpZero for 0
+  // e with |x| < 2^e (frexp convention); kExpZero for 0, kExpNonFinite for
+  // Inf and NaN
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const int be = (int)((b >> 52) & 0x7FF);
+  if (be == 0x7FF) return kExpNonFinite;
   if (be == 0) return (b << 1) == 0 ? kExpZero : -1022;  // subnormals: bound
   return be - 1022;
 }
@@ -645,8 +701,11 @@ __global__ void k_oz_globalexp(int64_t lena, const int32_t* __restrict__ rowexp,
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    misc[0] = red[0];
-    misc[1] = 0;
+    // misc[1], the sticky error word, is left alone; misc[2] flags an input
+    // holding Inf or NaN (the scatter then writes NaN, as FP64 would)
+    const int nonfinite = red[0] >= kExpNonFinite ? 1 : 0;
+    misc[0] = nonfinite ? 0 : red[0];
+    misc[2] = nonfinite;
   }
 }
 
@@ -655,10 +714,11 @@ __global__ void k_oz_fixed(int64_t n, const double2* __restrict__ psi,
                            const int32_t* __restrict__ misc,
                            longlong2* __restrict__ psix) {
   const int g0 = misc[0];
+  const bool skip = misc[2] != 0;  // non-finite input: the output is NaN anyway
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     longlong2 o = make_longlong2(0, 0);
-    if (g0 > kExpZero) {
+    if (g0 > kExpZero && !skip) {
       const double2 v = psi[i];
       o.x = __double2ll_rn(ldexp(v.x, 62 - g0));
       o.y = __double2ll_rn(ldexp(v.y, 62 - g0));
@@ -691,10 +751,14 @@ __global__ void __launch_bounds__(256) k_oz_scatter_csr(
     const int32_t* __restrict__ tabA, const int32_t* __restrict__ boff,
     const int2* __restrict__ bent, const float4* __restrict__ G,
     const double2* __restrict__ psi, double2 alpha, double2 beta, int init,
-    double2* __restrict__ sigma) {
+    const int32_t* __restrict__ misc, double2* __restrict__ sigma) {
   const int64_t a = blockIdx.y;
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= lenb) return;
+  if (misc[2]) {  // psi holds Inf or NaN
+    sigma[a * lenb + b] = make_double2(CUDART_NAN, CUDART_NAN);
+    return;
+  }
   float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
   if (b >= c0 && b < c0 + w) {
     for (int p = 0; p < P; ++p) {
@@ -742,10 +806,14 @@ __global__ void __launch_bounds__(256) k_oz_scatter(
     const int32_t* __restrict__ tabA,
     const int32_t* __restrict__ tabB, const float4* __restrict__ G,
     const double2* __restrict__ psi, double2 alpha, double2 beta, int init,
-    double2* __restrict__ sigma) {
+    const int32_t* __restrict__ misc, double2* __restrict__ sigma) {
   const int64_t a = blockIdx.y;
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= lenb) return;
+  if (misc[2]) {  // psi holds Inf or NaN
+    sigma[a * lenb + b] = make_double2(CUDART_NAN, CUDART_NAN);
+    return;
+  }
   const bool inblk = b >= c0 && b < c0 + w;
   float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
   for (int p = 0; p < P; ++p) {
@@ -855,10 +923,10 @@ static int plan_create(fqegpu_ham h) {
       }
     }
   }
-  FQE_CUDA(cudaMalloc(&pl->d_vslices, sizeof(__nv_bfloat16) * sl.size()));
+  FQE_CUDA(dev_alloc(&pl->d_vslices, sizeof(__nv_bfloat16) * sl.size()));
   FQE_CUDA(cudaMemcpy(pl->d_vslices, sl.data(), sizeof(__nv_bfloat16) * sl.size(),
                       cudaMemcpyHostToDevice));
-  FQE_CUDA(cudaMalloc(&pl->d_vexp, sizeof(int32_t) * vexp.size()));
+  FQE_CUDA(dev_alloc(&pl->d_vexp, sizeof(int32_t) * vexp.size()));
   FQE_CUDA(cudaMemcpy(pl->d_vexp, vexp.data(), sizeof(int32_t) * vexp.size(),
                       cudaMemcpyHostToDevice));
   const int64_t lena = h->g->a.len, lenb = h->g->b.len, N = lena * lenb;
@@ -872,17 +940,21 @@ static int plan_create(fqegpu_ham h) {
     wb = std::max<int64_t>(kDets, wb / kDets * kDets);
   }
   pl->wb = wb;
-  FQE_CUDA(cudaMalloc(&pl->d_psix, sizeof(longlong2) * N));
-  FQE_CUDA(cudaMalloc(&pl->d_rowexp, sizeof(int32_t) * lena));
-  FQE_CUDA(cudaMalloc(&pl->d_misc, sizeof(int32_t) * 4));
-  FQE_CUDA(cudaMalloc(&pl->d_G, sizeof(float4) * (size_t)P * lena * wb));
-  FQE_CUDA(cudaMalloc(&pl->d_bexp, sizeof(uchar2) * N));
+  FQE_CUDA(dev_alloc(&pl->d_psix, sizeof(longlong2) * N));
+  FQE_CUDA(dev_alloc(&pl->d_rowexp, sizeof(int32_t) * lena));
+  FQE_CUDA(dev_alloc(&pl->d_misc, sizeof(int32_t) * 4));
+  FQE_CUDA(cudaMemset(pl->d_misc, 0, sizeof(int32_t) * 4));
+  FQE_CUDA(cudaHostAlloc(&pl->h_err, sizeof(int32_t), cudaHostAllocDefault));
+  *pl->h_err = 0;
+  FQE_CUDA(cudaEventCreateWithFlags(&pl->err_ev, cudaEventDisableTiming));
+  FQE_CUDA(dev_alloc(&pl->d_G, sizeof(float4) * (size_t)P * lena * wb));
+  FQE_CUDA(dev_alloc(&pl->d_bexp, sizeof(uchar2) * N));
   {
     const bool tri = h->compressed;
     const int32_t* ta = tri ? h->g->a.tab_tri : h->g->a.tab_full;
     const int32_t* tb = tri ? h->g->b.tab_tri : h->g->b.tab_full;
-    FQE_CUDA(cudaMalloc(&pl->d_tabTA, sizeof(int32_t) * (size_t)lena * KP));
-    FQE_CUDA(cudaMalloc(&pl->d_tabTB, sizeof(int32_t) * (size_t)lenb * KP));
+    FQE_CUDA(dev_alloc(&pl->d_tabTA, sizeof(int32_t) * (size_t)lena * KP));
+    FQE_CUDA(dev_alloc(&pl->d_tabTB, sizeof(int32_t) * (size_t)lenb * KP));
     k_oz_transpose_tab<<<(unsigned)((lena * KP + 255) / 256), 256>>>(P, KP, lena, ta,
                                                                      pl->d_tabTA);
     k_oz_transpose_tab<<<(unsigned)((lenb * KP + 255) / 256), 256>>>(P, KP, lenb, tb,
@@ -917,10 +989,10 @@ static int plan_create(fqegpu_ham h) {
         const int32_t v = (int32_t)(src - k * wb + 1);
         ent[(size_t)cur[(size_t)k * row + b]++] = make_int2(p, cb > 0 ? v : -v);
       }
-    FQE_CUDA(cudaMalloc(&pl->d_boff, sizeof(int32_t) * off.size()));
+    FQE_CUDA(dev_alloc(&pl->d_boff, sizeof(int32_t) * off.size()));
     FQE_CUDA(cudaMemcpy(pl->d_boff, off.data(), sizeof(int32_t) * off.size(),
                         cudaMemcpyHostToDevice));
-    FQE_CUDA(cudaMalloc(&pl->d_bent, sizeof(int2) * std::max<size_t>(ent.size(), 1)));
+    FQE_CUDA(dev_alloc(&pl->d_bent, sizeof(int2) * std::max<size_t>(ent.size(), 1)));
     if (!ent.empty())
       FQE_CUDA(cudaMemcpy(pl->d_bent, ent.data(), sizeof(int2) * ent.size(),
                           cudaMemcpyHostToDevice));
@@ -928,7 +1000,7 @@ static int plan_create(fqegpu_ham h) {
   const int64_t ntiles = lena * ((wb + kDets - 1) / kDets);  // tiles of the widest block
   const int64_t npairs = (ntiles + 1) / 2;
   const size_t dsl = sizeof(__nv_bfloat16) * (size_t)npairs * 2 * kSlices * kN * KP;
-  FQE_CUDA(cudaMalloc(&pl->d_dslices, dsl));
+  FQE_CUDA(dev_alloc(&pl->d_dslices, dsl));
   FQE_CUDA(cudaMemset(pl->d_dslices, 0, dsl));  // an unpaired last tile reads zeros
   FQE_CUDA(cudaDeviceGetAttribute(&pl->nsm, cudaDevAttrMultiProcessorCount, dev));
   // as many slice slots as shared memory holds after the V slices
@@ -941,10 +1013,57 @@ static int plan_create(fqegpu_ham h) {
   return FQEGPU_OK;
 }
 
-int ozaki_error_flag(fqegpu_ham h, int32_t* out) {
-  *out = 0;
-  if (!h->oz) return FQEGPU_OK;
-  FQE_CUDA(cudaMemcpy(out, h->oz->d_misc + 1, sizeof(int32_t), cudaMemcpyDeviceToHost));
+// Blocking check of the tensor-core path's sticky error word: waits for
+// `st`, reads the word, clears it, and reports FQEGPU_ERR_TIMEOUT when a
+// bounded wait of any apply since the last check gave up.
+int ozaki_check(fqegpu_ham h, cudaStream_t st) {
+  OzakiPlan* pl = h->oz;
+  if (!pl) return FQEGPU_OK;
+  FQE_CUDA(cudaStreamSynchronize(st));
+  if (pl->err_pending) FQE_CUDA(cudaEventSynchronize(pl->err_ev));
+  pl->err_pending = false;
+  int32_t v = 0;
+  FQE_CUDA(cudaMemcpy(&v, pl->d_misc + 1, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (v != 0) {
+    FQE_CUDA(cudaMemset(pl->d_misc + 1, 0, sizeof(int32_t)));
+    *pl->h_err = 0;
+    set_error("tensor-core contraction: a bounded wait gave up (role %d)", v);
+    return FQEGPU_ERR_TIMEOUT;
+  }
+  return FQEGPU_OK;
+}
+
+// Non-blocking poll: if the last apply's error word has reached the host and
+// is set, clear it and report the timeout now.
+static int ozaki_poll(OzakiPlan* pl, cudaStream_t st) {
+  if (!pl->err_pending) return FQEGPU_OK;
+  const cudaError_t q = cudaEventQuery(pl->err_ev);
+  if (q == cudaErrorNotReady) return FQEGPU_OK;
+  FQE_CUDA(q);
+  pl->err_pending = false;
+  const int32_t v = *pl->h_err;
+  if (v == 0) return FQEGPU_OK;
+  *pl->h_err = 0;
+  FQE_CUDA(cudaMemsetAsync(pl->d_misc + 1, 0, sizeof(int32_t), st));
+  set_error("tensor-core contraction of an earlier apply: a bounded wait gave up (role %d)", v);
+  return FQEGPU_ERR_TIMEOUT;
+}
+
+int ozaki_prepare(fqegpu_ham h) {
+  if (h->zero || h->onebody || !h->real || h->P > 192) return FQEGPU_ERR_UNSUPPORTED;
+  if (h->g->a.len > 65535) return FQEGPU_ERR_UNSUPPORTED;
+  if (!h->oz) {
+    const int s = plan_create(h);
+    if (s == FQEGPU_ERR_UNSUPPORTED && !h->oz) return FQEGPU_ERR_UNSUPPORTED;
+    FQE_TRY(s);
+  }
+  return FQEGPU_OK;
+}
+
+int ozaki_set_test_injection(fqegpu_ham h, long long wait_cycles, int skip_slot) {
+  FQE_TRY(ozaki_prepare(h));
+  h->oz->wait_cycles = wait_cycles > 0 ? wait_cycles : kWaitCycles;
+  h->oz->skip_slot = skip_slot;
   return FQEGPU_OK;
 }
 
@@ -963,6 +1082,8 @@ void ozaki_destroy(fqegpu_ham h) {
   cudaFree(pl->d_dslices);
   cudaFree(pl->d_boff);
   cudaFree(pl->d_bent);
+  if (pl->h_err) cudaFreeHost(pl->h_err);
+  if (pl->err_ev) cudaEventDestroy(pl->err_ev);
   delete pl;
   h->oz = nullptr;
 }
@@ -980,12 +1101,13 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
               (long long)lena);
     return FQEGPU_ERR_UNSUPPORTED;
   }
-  if (!h->oz) {
-    const int s = plan_create(h);
-    if (s == FQEGPU_ERR_UNSUPPORTED && !h->oz) return apply_fp64(h, psi, sigma, alpha, beta, st);
+  {
+    const int s = ozaki_prepare(h);
+    if (s == FQEGPU_ERR_UNSUPPORTED) return apply_fp64(h, psi, sigma, alpha, beta, st);
     FQE_TRY(s);
   }
   OzakiPlan* pl = h->oz;
+  if (!h->defer_check) FQE_TRY(ozaki_poll(pl, st));
   const bool tri = h->compressed;
   const int32_t* tabA = tri ? g->a.tab_tri : g->a.tab_full;
   const int32_t* tabB = tri ? g->b.tab_tri : g->b.tab_full;
@@ -1013,6 +1135,8 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   A.tabTB = pl->d_tabTB;
   A.dslices = pl->d_dslices;
   A.err = pl->d_misc + 1;
+  A.wait_cycles = pl->wait_cycles;
+  A.skip_slot = pl->skip_slot;
   const size_t vel = (size_t)pl->NP * pl->KP;
   const double2 al = zmul_host(alpha, h->phase);
   int blk = 0;
@@ -1041,21 +1165,21 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
     if (pl->d_boff)
       k_oz_scatter_csr<<<sg, 256, 0, st>>>(pl->P, lena, lenb, c0, w, pl->wb, tabA,
                                            pl->d_boff + (size_t)blk * (lenb + 1), pl->d_bent,
-                                           pl->d_G, psi, al, beta, blk == 0 ? 1 : 0, sigma);
+                                           pl->d_G, psi, al, beta, blk == 0 ? 1 : 0,
+                                           pl->d_misc, sigma);
     else
       k_oz_scatter<<<sg, 256, 0, st>>>(pl->P, lena, lenb, c0, w, pl->wb, tabA, tabB, pl->d_G,
-                                       psi, al, beta, blk == 0 ? 1 : 0, sigma);
+                                       psi, al, beta, blk == 0 ? 1 : 0, pl->d_misc, sigma);
     FQE_CUDA(cudaGetLastError());
     FQE_TRY(stage_mark(h, blk, 3, st));
   }
-  if (h->defer_check) return FQEGPU_OK;  // recorded into a graph
-  int32_t errv = 0;
-  FQE_CUDA(cudaMemcpyAsync(&errv, pl->d_misc + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  FQE_CUDA(cudaStreamSynchronize(st));
-  if (errv != 0) {
-    set_error("tensor-core contraction: a bounded wait gave up (role %d)", errv);
-    return FQEGPU_ERR_TIMEOUT;
-  }
+  if (h->defer_check) return FQEGPU_OK;  // recorded into a graph: checked by its owner
+  // no host synchronisation: the sticky error word travels to pinned memory
+  // behind the apply; the next apply polls it, fqegpu_ham_check waits for it
+  FQE_CUDA(cudaMemcpyAsync(pl->h_err, pl->d_misc + 1, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                           st));
+  FQE_CUDA(cudaEventRecord(pl->err_ev, st));
+  pl->err_pending = true;
   return FQEGPU_OK;
 }
 

@@ -3,6 +3,7 @@
 //
 // Reductions are two-pass with a fixed grid and a fixed summation tree, so a
 // result does not depend on scheduling (bit-reproducible run to run).
+#include <atomic>
 #include <cstdarg>
 #include <cstring>
 
@@ -20,6 +21,19 @@ void set_error(const char* fmt, ...) {
 }
 
 void clear_error() { g_err[0] = 0; }
+
+static std::atomic<int> g_fail_allocs{0};
+
+cudaError_t dev_alloc_bytes(void** p, size_t bytes) {
+  int n = g_fail_allocs.load();
+  while (n > 0) {
+    if (g_fail_allocs.compare_exchange_weak(n, n - 1)) {
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+  }
+  return cudaMalloc(p, bytes);
+}
 
 constexpr int kRedBlocks = 1024;
 constexpr int kRedThreads = 256;
@@ -227,6 +241,13 @@ extern "C" int fqegpu_last_error(char* buf, int buflen) {
   if (!buf || buflen <= 0) return FQEGPU_ERR_INVALID;
   strncpy(buf, g_err, (size_t)buflen - 1);
   buf[buflen - 1] = 0;
+  return FQEGPU_OK;
+}
+
+extern "C" int fqegpu_debug_fail_allocs(int count) {
+  clear_error();
+  FQE_CHECK_ARG(count >= 0, "count must be >= 0");
+  g_fail_allocs.store(count);
   return FQEGPU_OK;
 }
 

@@ -49,6 +49,9 @@ _SIGNATURES = {
     "fqegpu_ham_stage_ms": [_P, _P],
     "fqegpu_apply": [_P, _P, _P, _D, _D, _D, _D, _I, _P],
     "fqegpu_apply_host": [_P, _P, _P, _D, _D, _D, _D, _I],
+    "fqegpu_ham_check": [_P, _P],
+    "fqegpu_ham_test_injection": [_P, _L, _I],
+    "fqegpu_debug_fail_allocs": [_I],
     "fqegpu_apply_noalloc": [_I, _I, _I, _P, _P, _P, _P, _D, _D, _D, _D, _P],
     "fqegpu_make_dvec": [_P, _P, _P, _P],
     "fqegpu_make_coeff": [_P, _P, _P, _I, _P],
@@ -68,6 +71,9 @@ _SIGNATURES = {
     "fqegpu_batch_launch": [_P, _P],
     "fqegpu_batch_check": [_P, _P],
     "fqegpu_batch_destroy": [_P],
+    "fqegpu_batch_taylor_create": [_I, _P, _P, _D, _D, _I, _I, _P,
+                                   ctypes.POINTER(_P)],
+    "fqegpu_batch_taylor_terms": [_P, _P, _P],
     "fqegpu_precondition": [_L, _P, _P, _D, _D, _P, _P],
     "fqegpu_mlp_create": [ctypes.POINTER(_P)],
     "fqegpu_mlp_destroy": [_P],

@@ -151,6 +151,11 @@ class _Operator:
     def apply(self, v: torch.Tensor) -> torch.Tensor:
         return self.apply_shifted(v, 0.0)
 
+    def check(self) -> None:
+        """Waits for the applies so far and raises TimeoutError if a
+        tensor-core apply gave up a bounded wait (fqegpu_ham_check)."""
+        _lib.call("fqegpu_ham_check", self.ham.handle, _stream())
+
     def apply_shifted(self, v: torch.Tensor, shift: float) -> torch.Tensor:
         """(H + shift) v."""
         out = torch.empty_like(v)
@@ -227,6 +232,7 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
     X: List[torch.Tensor] = []
     it = 0
     for it in range(1, max_iter + 1):
+        op.check()  # the subspace sums below synchronise anyway
         m = len(V)
         Tn = numpy.zeros((m, m), dtype=numpy.complex128)
         Tn[:T.shape[0], :T.shape[1]] = T
@@ -282,6 +288,7 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
                     added += 1
         if added == 0:
             break
+    op.check()
     torch.cuda.synchronize()
     return DavidsonResult(fallback_iteration=fallback_it,
                           eigenvalues=numpy.array(theta), vectors=X[:nroots],

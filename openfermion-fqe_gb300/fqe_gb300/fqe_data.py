@@ -91,6 +91,12 @@ def ham_for(graph: FciGraph, h1, h2) -> _Ham:
     return ham
 
 
+def check_apply(ham: "_Ham") -> None:
+    """Waits for the current stream and raises TimeoutError if a tensor-core
+    apply of `ham` gave up a bounded device wait since the last check."""
+    _lib.call("fqegpu_ham_check", ham.handle, _stream())
+
+
 def rdm2_from_dvecs(dket: torch.Tensor, dbra: torch.Tensor,
                     rdm1: torch.Tensor) -> torch.Tensor:
     """rdm2 of FqeData.rdm12 (fqe_data.py:1762-1781) from the dvecs
@@ -263,6 +269,9 @@ class FqeData:
 
     def _run_apply(self, ham: _Ham, alpha=1.0, beta=0.0,
                    out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """alpha H coeff + beta coeff, asynchronous on the current stream (a
+        tensor-core timeout is reported by check_apply or the handle's next
+        apply)."""
         if out is None:
             out = torch.empty_like(self.coeff)
         a, b = complex(alpha), complex(beta)

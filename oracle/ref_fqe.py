@@ -30,7 +30,9 @@ import types
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(HERE, "_ref")
-REF_ROOT = os.environ.get("FQE_REFERENCE_ROOT", "/root/reference")
+# FQE_REFERENCE_ROOT, else a checkout named `reference` beside the repository
+REF_ROOT = os.environ.get("FQE_REFERENCE_ROOT") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
 REF_SRC = os.path.join(REF_ROOT, "src")
 
 

@@ -25,6 +25,9 @@ class _DenseOperator:
         self.applies += 1
         return (self.H @ v.reshape(-1)).reshape(self.shape)
 
+    def check(self):  # no device waits on the CPU
+        pass
+
 
 def _plain(r, theta, diag, graph, floor=1e-4):
     d = theta - diag

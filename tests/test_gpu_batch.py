@@ -47,3 +47,32 @@ def test_batch_matches_single_applies(gpu, precision):
                 assert torch.equal(one, s)
     finally:
         settings.precision = old
+
+
+def test_batch_follows_rebound_coefficients(gpu):
+    """FqeData.apply_inplace rebinds `coeff`; the batch keeps the tensors it
+    recorded alive and refreshes them from the sectors at launch."""
+    import gc
+    import torch
+    from fqe_gb300 import _lib
+    from fqe_gb300.batch import BatchApply
+    datas, arrays = _setup(gpu)
+    b = BatchApply(datas, arrays, precision="fp64")
+    recorded = b.psis[1]
+    datas[1].apply_inplace(arrays[1])  # coeff is now a new tensor
+    assert datas[1].coeff is not recorded
+    gc.collect()
+    torch.cuda.empty_cache()
+    b.launch()
+    b.check()
+    one = datas[1]._run_apply(b.hams[1])
+    torch.cuda.synchronize()
+    assert torch.equal(one, b.sigmas[1])
+    # the handles refuse to reallocate or free what the graph holds
+    with pytest.raises(ValueError, match="graph"):
+        _lib.call("fqegpu_ham_set_scratch_limit", b.hams[0].handle, 1 << 20)
+    assert _lib.load().fqegpu_ham_destroy(b.hams[0].handle) == _lib.ERR_INVALID
+    ham0 = b.hams[0]
+    del b
+    gc.collect()
+    _lib.call("fqegpu_ham_set_scratch_limit", ham0.handle, 1 << 30)  # released
