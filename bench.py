@@ -51,6 +51,8 @@ def set_workload(norb, nalpha, nbeta, nchol):
     NORB, NALPHA, NBETA, NCHOL = norb, nalpha, nbeta, nchol
     METRIC = f"H*psi det-updates/s at norb={norb}"
 UNIT = "det/s"
+# the tensor-core contraction: BF16 slices of D (psi's digits) and products
+OZ_DSLICES, OZ_PRODUCTS = 6, 20
 
 
 def peaks():
@@ -315,12 +317,13 @@ def run_gpu(args):
     # P x P x N; gather writes and scatter reads D/G at 16 B per element)
     KP = (P + 15) // 16 * 16
     if prec == "ozaki":
-        # slicing kernel writes 5 BF16 slices of 64 x KP per 32-det tile;
-        # contraction: 19 useful BF16 products of P x P x (2 real columns)
+        # slicing kernel writes 6 BF16 slices of 64 x KP per 32-det tile
+        # (reading psi's 24-byte digit words, once per determinant at least);
+        # contraction: 20 useful BF16 products of P x P x (2 real columns)
         ntiles = d.lena() * ((d.lenb() + 31) // 32)
-        slice_bytes = ntiles * 5 * 64 * KP * 2.0
-        contract_flops = 19 * 2.0 * P * P * 2.0 * n
-        gather_bytes = 16.0 * n + slice_bytes + 2.0 * n
+        slice_bytes = ntiles * OZ_DSLICES * 64 * KP * 2.0
+        contract_flops = OZ_PRODUCTS * 2.0 * P * P * 2.0 * n
+        gather_bytes = 16.0 * n + slice_bytes + 24.0 * n
     else:
         contract_flops = 2.0 * 2.0 * P * P * n
         gather_bytes = 16.0 * n + 16.0 * P * n
@@ -348,7 +351,7 @@ def run_gpu(args):
         # at norb 12 measured 0.98 x its algorithmic bytes (slice images read
         # once, G written once); scaled to this workload's algorithmic bytes
         ntiles = d.lena() * ((d.lenb() + 31) // 32)
-        images = 2 * ((ntiles + 1) // 2) * 5 * 64 * KP * 2.0
+        images = 2 * ((ntiles + 1) // 2) * OZ_DSLICES * 64 * KP * 2.0
         traffic = 0.98 * (images + 16.0 * P * n)
     elif prec == "ozaki" and names[dom] == "gather":
         # k_oz_slice DRAM bytes per launch: the norb-12 capture measured 1.386 GB
@@ -356,7 +359,7 @@ def run_gpu(args):
         # the images it writes; scaled to this workload's images (the small
         # exponent and fixed-point pre-passes of the stage are not included)
         ntiles = d.lena() * ((d.lenb() + 31) // 32)
-        traffic = 1.01 * 2 * ((ntiles + 1) // 2) * 5 * 64 * KP * 2.0
+        traffic = 1.01 * 2 * ((ntiles + 1) // 2) * OZ_DSLICES * 64 * KP * 2.0
     roofline = {"kernel": names[dom], "bound": dk["bound"],
                 "achieved": dk["achieved"], "peak": dk["peak"],
                 "unit": dk["unit"],

@@ -98,6 +98,20 @@ int fqegpu_graph_maps(fqegpu_graph g, int spin, int32_t *h_out);
  * symmetries, as fqe_data.py:658-681 does for real integrals. */
 int fqegpu_ham_create(fqegpu_graph g, const double *h_h1, const double *h_h2,
                       void *stream, fqegpu_ham *out);
+/* Spin-orbital (generalised) one- and two-body operator of the sector:
+ * h_h1 complex128 [2 norb][2 norb] (may be NULL), h_h2 complex128 [2 norb]^4
+ * (may be NULL: one-body), alpha spin orbitals first, in the reference's
+ * layouts.  Replaces FqeData._apply_array_spin12_lm (fqe_data.py:743-773:
+ * lm_apply_array12_same_spin_opt with the alpha-alpha and the beta-beta
+ * blocks, lm_apply_array12_diff_spin_opt with h2'[a,a,b,b] + h2'[b,b,a,a]^T)
+ * and _apply_array_spin1 (fqe_data.py:533-563: lm_apply_array1 with the
+ * alpha and the beta block).  h2'[I,J,K,L] = -h2[I,K,J,L], h1' = h1 +
+ * sum_K h2[I,K,K,J] over all 2 norb spin orbitals; blocks that move
+ * electrons between spins do not act on a sector and are ignored.  The
+ * handle works with fqegpu_apply (both precisions), fqegpu_taylor and the
+ * batches; not with fqegpu_diagonal. */
+int fqegpu_ham_create_spin(fqegpu_graph g, const double *h_h1,
+                           const double *h_h2, void *stream, fqegpu_ham *out);
 /* FQEGPU_ERR_INVALID (and nothing is freed) while a batch recorded with the
  * handle exists: destroy the batch first. */
 int fqegpu_ham_destroy(fqegpu_ham h);

@@ -226,24 +226,18 @@ __global__ void k_axpby(int64_t n, double2 beta, const double2* __restrict__ x,
                                             : cmul(beta, x[i]);
 }
 
-static const int32_t* tab_of(const SpinTables& t, bool tri) {
-  return tri ? t.tab_tri : t.tab_full;
-}
-
-int launch_gather(const fqegpu_graph_s* g, bool tri, int P, int64_t c0,
-                  int64_t w, const double2* psi, double2* D, cudaStream_t st) {
+int launch_gather(const fqegpu_graph_s* g, const int32_t* tabA, const int32_t* tabB, int P,
+                  int64_t c0, int64_t w, const double2* psi, double2* D, cudaStream_t st) {
   const int64_t lena = g->a.len, lenb = g->b.len;
   const int64_t rows = (int64_t)P * lena;
   if (rows == 0 || w == 0) return FQEGPU_OK;
-  k_gather_f64<<<(unsigned)rows, 256, 0, st>>>(P, lena, lenb, c0, w,
-                                               tab_of(g->a, tri), tab_of(g->b, tri),
-                                               psi, D);
+  k_gather_f64<<<(unsigned)rows, 256, 0, st>>>(P, lena, lenb, c0, w, tabA, tabB, psi, D);
   FQE_CUDA(cudaGetLastError());
   return FQEGPU_OK;
 }
 
-int launch_scatter(const fqegpu_graph_s* g, bool tri, int P, int64_t c0,
-                   int64_t w, const double2* G, const double2* psi,
+int launch_scatter(const fqegpu_graph_s* g, const int32_t* tabA, const int32_t* tabB, int P,
+                   int64_t c0, int64_t w, const double2* G, const double2* psi,
                    double2 alpha, double2 beta, bool init, double2* sigma,
                    cudaStream_t st) {
   const int64_t lena = g->a.len, lenb = g->b.len;
@@ -253,8 +247,8 @@ int launch_scatter(const fqegpu_graph_s* g, bool tri, int P, int64_t c0,
     return FQEGPU_ERR_UNSUPPORTED;
   }
   dim3 grid((unsigned)((lenb + 255) / 256), (unsigned)lena);
-  k_scatter<0><<<grid, 256, 0, st>>>(P, lena, lenb, c0, w, tab_of(g->a, tri),
-                                     tab_of(g->b, tri), G, psi, nullptr, nullptr,
+  k_scatter<0><<<grid, 256, 0, st>>>(P, lena, lenb, c0, w, tabA, tabB, G, psi, nullptr,
+                                     nullptr,
                                      alpha, beta, init ? 1 : 0, sigma);
   FQE_CUDA(cudaGetLastError());
   return FQEGPU_OK;
@@ -315,15 +309,12 @@ int apply_fp64(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   }
   if (h->onebody) {
     dim3 grid((unsigned)((lenb + 255) / 256), (unsigned)lena);
-    const bool tri = h->compressed;
     if (h->real) {
-      k_scatter<1><<<grid, 256, 0, st>>>(h->P, lena, lenb, 0, lenb,
-                                         tab_of(g->a, tri), tab_of(g->b, tri),
+      k_scatter<1><<<grid, 256, 0, st>>>(h->P, lena, lenb, 0, lenb, ham_tabA(h), ham_tabB(h),
                                          nullptr, psi, h->d_h1r, nullptr, al,
                                          beta, 1, sigma);
     } else {
-      k_scatter<2><<<grid, 256, 0, st>>>(h->P, lena, lenb, 0, lenb,
-                                         tab_of(g->a, tri), tab_of(g->b, tri),
+      k_scatter<2><<<grid, 256, 0, st>>>(h->P, lena, lenb, 0, lenb, ham_tabA(h), ham_tabB(h),
                                          nullptr, psi, nullptr, h->d_h1c, al,
                                          beta, 1, sigma);
     }
@@ -344,7 +335,7 @@ int apply_fp64(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   for (int64_t c0 = 0; c0 < lenb; c0 += w, ++blk) {
     const int64_t wb = std::min<int64_t>(w, lenb - c0);
     FQE_TRY(stage_mark(h, blk, 0, st));
-    FQE_TRY(launch_gather(g, h->compressed, h->P, c0, wb, psi, D, st));
+    FQE_TRY(launch_gather(g, ham_tabA(h), ham_tabB(h), h->P, c0, wb, psi, D, st));
     FQE_TRY(stage_mark(h, blk, 1, st));
     const int64_t ncol = lena * wb;
     dim3 grid((unsigned)((ncol + 63) / 64), (unsigned)((h->P + 63) / 64));
@@ -357,7 +348,7 @@ int apply_fp64(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
     }
     FQE_CUDA(cudaGetLastError());
     FQE_TRY(stage_mark(h, blk, 2, st));
-    FQE_TRY(launch_scatter(g, h->compressed, h->P, c0, wb, G, psi, al, beta,
+    FQE_TRY(launch_scatter(g, ham_tabA(h), ham_tabB(h), h->P, c0, wb, G, psi, al, beta,
                            single, sigma, st));
     FQE_TRY(stage_mark(h, blk, 3, st));
   }
@@ -378,8 +369,108 @@ int stage_mark(fqegpu_ham h, int blk, int k, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
-// Host-side preparation of (h1, h2) (fqe_data.py:691-693 and the compressed
-// branch's symmetry assumption, fqe_data.py:658-681); declared in ham.cuh.
+// Host-side preparation of the pair matrix; declared in ham.cuh.
+//
+// `full` holds the operator in the uncompressed pair space of `nspin` blocks
+// (pair (s, i, j) at s n^2 + i n + j; a [P][P] matrix, or a [P] weight vector
+// for one-body operators).  Factors out a global phase when what remains is
+// real, tests the real-orbital pair symmetry (i <-> j and k <-> l inside
+// every block) and, when it holds, compresses each block to the n(n+1)/2
+// pairs p = tri(i, j) (E_p = E_ij + E_ji), as fqe_data.py:658-681 does.
+static void finish_pairs(int n, int nspin, const std::vector<zd>& full, PairMatrix& out) {
+  const int n2 = n * n;
+  const int PP = nspin * n2;
+  double maxabs = 0.0;
+  size_t imax = 0;
+  for (size_t k = 0; k < full.size(); ++k) {
+    const double v = std::abs(full[k]);
+    if (v > maxabs) {
+      maxabs = v;
+      imax = k;
+    }
+  }
+  if (maxabs == 0.0) out.zero = true;
+  if (out.zero) return;
+  zd ph = full[imax] / maxabs;
+  if (ph.real() == 0.0 || ph.imag() == 0.0) ph = zd(ph.real() == 0.0 ? 0.0 : (ph.real() > 0 ? 1.0 : -1.0),
+                                                    ph.imag() == 0.0 ? 0.0 : (ph.imag() > 0 ? 1.0 : -1.0));
+  const double tol = 64.0 * DBL_EPSILON * maxabs;
+  bool real = true;
+  std::vector<zd> rot(full.size());
+  for (size_t k = 0; k < full.size(); ++k) {
+    rot[k] = full[k] * std::conj(ph);
+    if (std::abs(rot[k].imag()) > tol) real = false;
+  }
+  out.real = real;
+  out.phase = real ? make_double2(ph.real(), ph.imag()) : make_double2(1.0, 0.0);
+  const std::vector<zd>& src = real ? rot : full;
+  // index of pair (s, i, j) in the uncompressed space
+  auto up = [&](int s, int i, int j) { return (size_t)s * n2 + (size_t)i * n + j; };
+  bool sym = true;
+  if (out.onebody) {
+    for (int s = 0; s < nspin && sym; ++s)
+      for (int i = 0; i < n && sym; ++i)
+        for (int j = 0; j < i && sym; ++j)
+          if (std::abs(src[up(s, i, j)] - src[up(s, j, i)]) > tol) sym = false;
+  } else {
+    for (int s = 0; s < nspin && sym; ++s)
+      for (int i = 0; i < n && sym; ++i)
+        for (int j = 0; j < n && sym; ++j)
+          for (int t = 0; t < nspin && sym; ++t)
+            for (int k = 0; k < n && sym; ++k)
+              for (int l = 0; l < n; ++l) {
+                const zd v = src[up(s, i, j) * PP + up(t, k, l)];
+                if (std::abs(v - src[up(s, j, i) * PP + up(t, k, l)]) > tol ||
+                    std::abs(v - src[up(s, i, j) * PP + up(t, l, k)]) > tol) {
+                  sym = false;
+                  break;
+                }
+              }
+  }
+  out.compressed = sym;
+  const int per = sym ? n * (n + 1) / 2 : n2;  // pairs per spin block
+  const int P = nspin * per;
+  out.P = P;
+  // compressed or uncompressed pair p -> (s, i, j)
+  auto pair_of = [&](int p, int& sp, int& i, int& j) {
+    sp = p / per;
+    const int r = p - sp * per;
+    if (!sym) {
+      i = r / n;
+      j = r % n;
+      return;
+    }
+    int a = 0;
+    while ((a + 1) * (a + 2) / 2 <= r) ++a;
+    i = a;
+    j = r - a * (a + 1) / 2;
+  };
+  if (out.onebody) {
+    if (real) out.vr.resize(P); else out.vc.resize(P);
+    for (int p = 0; p < P; ++p) {
+      int sp, i, j;
+      pair_of(p, sp, i, j);
+      const zd v = src[up(sp, i, j)];
+      if (real) out.vr[p] = v.real();
+      else out.vc[p] = make_double2(v.real(), v.imag());
+    }
+    return;
+  }
+  if (real) out.vr.resize((size_t)P * P); else out.vc.resize((size_t)P * P);
+  for (int p = 0; p < P; ++p) {
+    int sp, i, j;
+    pair_of(p, sp, i, j);
+    for (int q = 0; q < P; ++q) {
+      int sq, k, l;
+      pair_of(q, sq, k, l);
+      const zd v = src[up(sp, i, j) * PP + up(sq, k, l)];
+      if (real) out.vr[(size_t)p * P + q] = v.real();
+      else out.vc[(size_t)p * P + q] = make_double2(v.real(), v.imag());
+    }
+  }
+}
+
+// Restricted (spin-free) operator (fqe_data.py:691-693).
 void prepare_pairs(int n, int nele, const zd* H1, const zd* H2, PairMatrix& out) {
   const int n2 = n * n;
   out = PairMatrix();
@@ -403,7 +494,8 @@ void prepare_pairs(int n, int nele, const zd* H1, const zd* H2, PairMatrix& out)
         out.h1p[i * n + j] += s;
       }
   }
-  // Full pair matrix (or one-body vector) in the uncompressed space.
+  // Full pair matrix (or one-body vector) in the uncompressed space: the
+  // one-body part rides in the contraction as h1'[ij] delta_kl / N_e
   std::vector<zd> full;
   if (out.onebody) {
     full = out.h1p;
@@ -415,92 +507,101 @@ void prepare_pairs(int n, int nele, const zd* H1, const zd* H2, PairMatrix& out)
         for (int k = 0; k < n; ++k) full[(size_t)ij * n2 + (k * n + k)] += out.h1p[ij] * inv;
     }
   }
-  double maxabs = 0.0;
-  size_t imax = 0;
-  for (size_t k = 0; k < full.size(); ++k) {
-    const double v = std::abs(full[k]);
-    if (v > maxabs) {
-      maxabs = v;
-      imax = k;
-    }
-  }
-  out.zero = (maxabs == 0.0) || nele == 0 || n == 0;
-  if (out.zero) return;
-  // Factor out a global phase; real if what remains has no imaginary part.
-  zd ph = full[imax] / maxabs;
-  if (ph.real() == 0.0 || ph.imag() == 0.0) ph = zd(ph.real() == 0.0 ? 0.0 : (ph.real() > 0 ? 1.0 : -1.0),
-                                                    ph.imag() == 0.0 ? 0.0 : (ph.imag() > 0 ? 1.0 : -1.0));
-  const double tol = 64.0 * DBL_EPSILON * maxabs;
-  bool real = true;
-  std::vector<zd> rot(full.size());
-  for (size_t k = 0; k < full.size(); ++k) {
-    rot[k] = full[k] * std::conj(ph);
-    if (std::abs(rot[k].imag()) > tol) real = false;
-  }
-  out.real = real;
-  out.phase = real ? make_double2(ph.real(), ph.imag()) : make_double2(1.0, 0.0);
-  const std::vector<zd>& src = real ? rot : full;
-  // Compressible: symmetric under i<->j (and k<->l for the pair matrix).
-  bool sym = true;
-  if (out.onebody) {
-    for (int i = 0; i < n && sym; ++i)
-      for (int j = 0; j < i && sym; ++j)
-        if (std::abs(src[i * n + j] - src[j * n + i]) > tol) sym = false;
-  } else {
-    for (int i = 0; i < n && sym; ++i)
-      for (int j = 0; j < n && sym; ++j)
-        for (int k = 0; k < n && sym; ++k)
-          for (int l = 0; l < n; ++l) {
-            const zd v = src[(size_t)(i * n + j) * n2 + k * n + l];
-            if (std::abs(v - src[(size_t)(j * n + i) * n2 + k * n + l]) > tol ||
-                std::abs(v - src[(size_t)(i * n + j) * n2 + l * n + k]) > tol) {
-              sym = false;
-              break;
-            }
-          }
-  }
-  out.compressed = sym;
-  const int P = sym ? n * (n + 1) / 2 : n2;
-  out.P = P;
-  auto pair_of = [&](int p, int& i, int& j) {
-    if (!sym) {
-      i = p / n;
-      j = p % n;
-      return;
-    }
-    int a = 0;
-    while ((a + 1) * (a + 2) / 2 <= p) ++a;
-    i = a;
-    j = p - a * (a + 1) / 2;
-  };
-  if (out.onebody) {
-    if (real) out.vr.resize(P); else out.vc.resize(P);
-    for (int p = 0; p < P; ++p) {
-      int i, j;
-      pair_of(p, i, j);
-      const zd v = src[i * n + j];
-      if (real) out.vr[p] = v.real();
-      else out.vc[p] = make_double2(v.real(), v.imag());
-    }
-    return;
-  }
-  if (real) out.vr.resize((size_t)P * P); else out.vc.resize((size_t)P * P);
-  for (int p = 0; p < P; ++p) {
-    int i, j;
-    pair_of(p, i, j);
-    for (int q = 0; q < P; ++q) {
-      int k, l;
-      pair_of(q, k, l);
-      const zd v = src[(size_t)(i * n + j) * n2 + k * n + l];
-      if (real) out.vr[(size_t)p * P + q] = v.real();
-      else out.vc[(size_t)p * P + q] = make_double2(v.real(), v.imag());
-    }
-  }
+  out.zero = nele == 0 || n == 0;
+  finish_pairs(n, 1, full, out);
 }
+
+// Spin-orbital operator (h1 [2n][2n], h2 [2n]^4, alpha orbitals first), as
+// _apply_array_spin12_lm (fqe_data.py:743-773) and _apply_array_spin1
+// (:533-563) define it: h2'[I,J,K,L] = -h2[I,K,J,L] and h1' = h1 + sum_K
+// h2[I,K,K,J] over all 2n spin orbitals; in the pair space of alpha pairs
+// (s = 0) followed by beta pairs (s = 1), with E_(s,ij) = E^s_ij,
+//   W[(s,ij)][(t,kl)] = h2'[sn+i, sn+j, tn+k, tn+l]
+//                       + delta_st delta_kl h1'[sn+i, sn+j] / N_s
+// (sum_k E^s_kk = N_s on the sector), so sigma = sum_pq W[p][q] E_p E_q psi,
+// the operator the reference's halffilling branch builds from
+// calculate_dvec_spin (fqe_data.py:725-741).  Blocks that move electrons
+// between spins do not act on a sector and are ignored, as there.
+void prepare_pairs_spin(int n, int na, int nb, const zd* H1, const zd* H2, PairMatrix& out) {
+  const int m = 2 * n, n2 = n * n, PP = 2 * n2;
+  out = PairMatrix();
+  out.onebody = (H2 == nullptr);
+  std::vector<zd> h1p((size_t)m * m, zd(0.0, 0.0));
+  if (H1)
+    for (int k = 0; k < m * m; ++k) h1p[k] = H1[k];
+  auto h2 = [&](int I, int J, int K, int L) {
+    return H2[(((size_t)I * m + J) * m + K) * m + L];
+  };
+  if (!out.onebody)
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) {
+        zd s(0.0, 0.0);
+        for (int k = 0; k < m; ++k) s += h2(i, k, k, j);
+        h1p[(size_t)i * m + j] += s;
+      }
+  std::vector<zd> full;
+  const int nel[2] = {na, nb};
+  if (out.onebody) {
+    full.assign((size_t)PP, zd(0.0, 0.0));
+    for (int s = 0; s < 2; ++s)
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+          full[(size_t)s * n2 + i * n + j] = h1p[(size_t)(s * n + i) * m + s * n + j];
+  } else {
+    full.assign((size_t)PP * PP, zd(0.0, 0.0));
+    for (int s = 0; s < 2; ++s)
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          const size_t row = ((size_t)s * n2 + i * n + j) * PP;
+          for (int t = 0; t < 2; ++t)
+            for (int k = 0; k < n; ++k)
+              for (int l = 0; l < n; ++l)
+                full[row + (size_t)t * n2 + k * n + l] =
+                    -h2(s * n + i, t * n + k, s * n + j, t * n + l);
+          if (nel[s] > 0) {
+            const zd w = h1p[(size_t)(s * n + i) * m + s * n + j] / (double)nel[s];
+            for (int k = 0; k < n; ++k) full[row + (size_t)s * n2 + k * n + k] += w;
+          }
+        }
+  }
+  out.zero = (na + nb == 0) || n == 0;
+  finish_pairs(n, 2, full, out);
+}
+
+static int upload_pairs(fqegpu_ham h, PairMatrix& pm);
 
 static int prepare(fqegpu_ham h, const double* h_h1, const double* h_h2) {
   PairMatrix pm;
   prepare_pairs(h->norb, h->nele, (const zd*)h_h1, (const zd*)h_h2, pm);
+  return upload_pairs(h, pm);
+}
+
+// Spin-orbital operator: the pair matrix of prepare_pairs_spin and the
+// handle's own tables [P][len] (alpha pairs read the alpha table, beta pairs
+// the beta table; the other spin's rows are zero).
+static int prepare_spin(fqegpu_ham h, const double* h_h1, const double* h_h2) {
+  PairMatrix pm;
+  const fqegpu_graph_s* g = h->g;
+  prepare_pairs_spin(h->norb, g->nalpha, g->nbeta, (const zd*)h_h1, (const zd*)h_h2, pm);
+  h->spin = true;
+  FQE_TRY(upload_pairs(h, pm));
+  if (h->zero) return FQEGPU_OK;
+  const int P = h->P, per = P / 2;
+  const int64_t lena = g->a.len, lenb = g->b.len;
+  const int32_t* srcA = h->compressed ? g->a.tab_tri : g->a.tab_full;
+  const int32_t* srcB = h->compressed ? g->b.tab_tri : g->b.tab_full;
+  FQE_CUDA(dev_alloc(&h->d_tabA, sizeof(int32_t) * (size_t)P * (size_t)std::max<int64_t>(lena, 1)));
+  FQE_CUDA(dev_alloc(&h->d_tabB, sizeof(int32_t) * (size_t)P * (size_t)std::max<int64_t>(lenb, 1)));
+  FQE_CUDA(cudaMemset(h->d_tabA, 0, sizeof(int32_t) * (size_t)P * lena));
+  FQE_CUDA(cudaMemset(h->d_tabB, 0, sizeof(int32_t) * (size_t)P * lenb));
+  FQE_CUDA(cudaMemcpy(h->d_tabA, srcA, sizeof(int32_t) * (size_t)per * lena,
+                      cudaMemcpyDeviceToDevice));
+  FQE_CUDA(cudaMemcpy(h->d_tabB + (size_t)per * lenb, srcB, sizeof(int32_t) * (size_t)per * lenb,
+                      cudaMemcpyDeviceToDevice));
+  return FQEGPU_OK;
+}
+
+static int upload_pairs(fqegpu_ham h, PairMatrix& pm) {
   h->h1p = std::move(pm.h1p);
   h->v2 = std::move(pm.v2);
   h->onebody = pm.onebody;
@@ -547,6 +648,8 @@ static void ham_free(fqegpu_ham h) {
   cudaFree(h->d_ws);
   cudaFree(h->d_vec);
   cudaFree(h->d_red);
+  cudaFree(h->d_tabA);
+  cudaFree(h->d_tabB);
   delete h;
 }
 
@@ -572,6 +675,31 @@ extern "C" int fqegpu_ham_create(fqegpu_graph g, const double* h_h1,
   if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) fr = (size_t)8 << 30;
   h->scratch_limit = (int64_t)(0.4 * (double)fr);
   const int s = prepare(h, h_h1, h_h2);
+  if (s != FQEGPU_OK) {
+    ham_free(h);
+    return s;
+  }
+  *out = h;
+  return FQEGPU_OK;
+}
+
+extern "C" int fqegpu_ham_create_spin(fqegpu_graph g, const double* h_h1,
+                                      const double* h_h2, void* stream, fqegpu_ham* out) {
+  clear_error();
+  (void)stream;
+  FQE_CHECK_ARG(g != nullptr && out != nullptr, "graph/out is NULL");
+  auto* h = new (std::nothrow) fqegpu_ham_s();
+  if (!h) {
+    set_error("host allocation failed");
+    return FQEGPU_ERR_NOMEM;
+  }
+  h->g = g;
+  h->norb = g->norb;
+  h->nele = g->nalpha + g->nbeta;
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) fr = (size_t)8 << 30;
+  h->scratch_limit = (int64_t)(0.4 * (double)fr);
+  const int s = prepare_spin(h, h_h1, h_h2);
   if (s != FQEGPU_OK) {
     ham_free(h);
     return s;
@@ -675,7 +803,7 @@ extern "C" int fqegpu_make_dvec(fqegpu_graph g, const double* d_psi,
   clear_error();
   FQE_CHECK_ARG(g && d_psi && d_dvec, "NULL argument");
   const int P = g->norb * g->norb;
-  return launch_gather(g, false, P, 0, g->b.len, (const double2*)d_psi,
+  return launch_gather(g, g->a.tab_full, g->b.tab_full, P, 0, g->b.len, (const double2*)d_psi,
                        (double2*)d_dvec, (cudaStream_t)stream);
 }
 
@@ -686,7 +814,7 @@ extern "C" int fqegpu_make_coeff(fqegpu_graph g, const double* d_dvec,
   const int P = g->norb * g->norb;
   if (P == 0) return FQEGPU_OK;
   // init=1 with beta=0 writes; init=0 accumulates into d_out.
-  return launch_scatter(g, false, P, 0, g->b.len, (const double2*)d_dvec,
+  return launch_scatter(g, g->a.tab_full, g->b.tab_full, P, 0, g->b.len, (const double2*)d_dvec,
                         (const double2*)d_out, make_double2(1.0, 0.0),
                         make_double2(0.0, 0.0), accumulate ? false : true,
                         (double2*)d_out, (cudaStream_t)stream);

@@ -225,6 +225,10 @@ extern "C" int fqegpu_diagonal_coulomb(fqegpu_graph g, const double* h_diag,
 extern "C" int fqegpu_diagonal(fqegpu_ham h, double* d_diag, void* stream) {
   clear_error();
   FQE_CHECK_ARG(h && d_diag, "NULL argument");
+  if (h->spin) {
+    set_error("the Slater-Condon diagonal is implemented for restricted operators only");
+    return FQEGPU_ERR_UNSUPPORTED;
+  }
   const int n = h->norb, n2 = n * n;
   std::vector<double2> d(n), A((size_t)n2), B((size_t)n2), R((size_t)n2);
   for (int i = 0; i < n; ++i) {

@@ -36,6 +36,11 @@ struct PairMatrix {
   std::vector<double2> vc;    // same, complex case
 };
 void prepare_pairs(int norb, int nele, const zd* H1, const zd* H2, PairMatrix& out);
+// The spin-orbital form (h1 [2 norb][2 norb], h2 [2 norb]^4, alpha orbitals
+// first; h2 may be NULL): pair space of alpha pairs then beta pairs, P =
+// 2 norb^2 (or 2 norb(norb+1)/2 compressed); h1p and v2 are left empty.
+void prepare_pairs_spin(int norb, int nalpha, int nbeta, const zd* H1, const zd* H2,
+                        PairMatrix& out);
 
 int axpy_async(int64_t n, double2 a, const double2* x, double2* y, cudaStream_t st);
 int scale_async(int64_t n, double2 a, double2* x, cudaStream_t st);
@@ -53,8 +58,14 @@ struct fqegpu_ham_s {
   bool onebody = false;     // no two-body tensor: sigma = sum_p h1_p E_p psi
   bool compressed = false;  // pair space p = tri(i, j)
   bool real = false;        // tensors are phase * (real tensor)
+  bool spin = false;        // spin-orbital operator: alpha pairs, then beta pairs
   double2 phase{1.0, 0.0};
   int P = 0;                // pair count
+  // Pair tables [P][len] of a spin-orbital operator (alpha rows zero in the
+  // beta table and vice versa), owned; NULL for a restricted operator, which
+  // reads the graph's tables.
+  int32_t* d_tabA = nullptr;
+  int32_t* d_tabB = nullptr;
   // Device copies, already divided by `phase` when real.
   double* d_Vr = nullptr;   // [P][P] real pair matrix (two-body, real)
   double2* d_Vc = nullptr;  // [P][P] complex pair matrix (two-body, complex)
@@ -89,6 +100,13 @@ struct fqegpu_ham_s {
 };
 
 namespace fqegpu {
+// The pair tables an apply of `h` reads: tab[p][string] = sign * (source + 1).
+inline const int32_t* ham_tabA(const fqegpu_ham_s* h) {
+  return h->d_tabA ? h->d_tabA : (h->compressed ? h->g->a.tab_tri : h->g->a.tab_full);
+}
+inline const int32_t* ham_tabB(const fqegpu_ham_s* h) {
+  return h->d_tabB ? h->d_tabB : (h->compressed ? h->g->b.tab_tri : h->g->b.tab_full);
+}
 inline double2 zmul_host(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -126,11 +144,12 @@ int taylor_phase(double2* psi, int64_t N, double time, double e0_re, double e0_i
                  cudaStream_t st);
 void taylor_destroy(fqegpu_ham h);
 constexpr size_t kTaylorStateHostBytes = 32;  // sizeof(TaylorState)
-// Gather / scatter building blocks (apply.cu).
-int launch_gather(const fqegpu_graph_s* g, bool tri, int P, int64_t c0,
-                  int64_t w, const double2* psi, double2* D, cudaStream_t st);
-int launch_scatter(const fqegpu_graph_s* g, bool tri, int P, int64_t c0,
-                   int64_t w, const double2* G, const double2* psi,
+// Gather / scatter building blocks (apply.cu) over the pair tables
+// tabA [P][lena], tabB [P][lenb] of the graph's sector.
+int launch_gather(const fqegpu_graph_s* g, const int32_t* tabA, const int32_t* tabB, int P,
+                  int64_t c0, int64_t w, const double2* psi, double2* D, cudaStream_t st);
+int launch_scatter(const fqegpu_graph_s* g, const int32_t* tabA, const int32_t* tabB, int P,
+                   int64_t c0, int64_t w, const double2* G, const double2* psi,
                    double2 alpha, double2 beta, bool init, double2* sigma,
                    cudaStream_t st);
 }  // namespace fqegpu

@@ -142,10 +142,12 @@ extern "C" int fqegpu_apply_noalloc(int norb, int nalpha, int nbeta, const doubl
   if (!single) FQE_TRY(launch_axpby(N, beta, psi, sigma, st));
   for (int64_t c0 = 0; c0 < lenb; c0 += w) {
     const int64_t wb = std::min<int64_t>(w, lenb - c0);
-    FQE_TRY(launch_gather(&g, hp.compressed, P, c0, wb, psi, D, st));
+    const int32_t* ta = hp.compressed ? g.a.tab_tri : g.a.tab_full;
+    const int32_t* tb = hp.compressed ? g.b.tab_tri : g.b.tab_full;
+    FQE_TRY(launch_gather(&g, ta, tb, P, c0, wb, psi, D, st));
     FQE_TRY(launch_pairgemm(P, lena * wb, hp.real ? static_cast<const double*>(dV) : nullptr,
                             hp.real ? nullptr : static_cast<const double2*>(dV), D, G, st));
-    FQE_TRY(launch_scatter(&g, hp.compressed, P, c0, wb, G, psi, al, beta, single, sigma, st));
+    FQE_TRY(launch_scatter(&g, ta, tb, P, c0, wb, G, psi, al, beta, single, sigma, st));
   }
   // hp's host buffers are read by the copy above; keep them alive until then
   FQE_CUDA(cudaStreamSynchronize(st));

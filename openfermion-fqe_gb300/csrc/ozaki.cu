@@ -5,31 +5,41 @@
 // GB300's FP64 pipe runs at ~1.1 TFLOP/s, so the FP64 operands are split into
 // BF16 slices and contracted on the 5th-generation tensor cores:
 //
-//   V[p][q] = 2^{eV(p)} sum_{k=1..5} v_k[p][q] 2^{-8k},  v_k in {-255..255}
-//   D[q][I] = 2^{E(I)}  sum_{k=1..5} d_k[q][I] 2^{-8k},  d_k in {-255..255}
+//   V[p][q] = 2^{eV(p)}   sum_{a=1..5} v_a[p][q] 2^{-8a},  v_a in {-255..255}
+//   D[q][I] = 2^{g0 + 1}  sum_{b=1..6} d_b[q][I] 2^{-8b},  d_b in {-256..256}
 //
-// (sign-magnitude bytes of 40-bit fixed-point values; eV(p) bounds row p of V,
-// E(I) bounds column I of D).  Every slice is stored as its true value
-// (byte * 2^{-8k}, exact in BF16), so every product lands on one absolute
-// scale and the products are grouped by level L = a + b into four TMEM
-// accumulators: L = 2, 3 and 4 sum integers times 2^{-8L} that stay below
-// 2^24 (exact in FP32; level 4 can only exceed it for near-saturated bytes);
-// L = 5..7 share one accumulator whose FP32 rounding sits ~2^-48 below the
-// leading term even after ~100 accumulation steps.  Levels >= 8 are
-// dropped: 19 BF16 products per tile.  (Merging level 4 into the last
-// accumulator left ~1e-10 of accumulated rounding; stopping at level 6
-// leaves ~1e-11.)  The
-// four accumulators are combined into an FP32 pair (hi + lo, ~48 bits) and
-// scaled by 2^{eV(p) + E(I)}.
+// V: sign-magnitude bytes of the 40-bit fixed-point rows (row exponent eV(p)).
+// D: psi is scaled by ONE global exponent g0 (max |Re|, |Im| of psi < 2^g0)
+// to a 47-bit fixed-point integer and cut once per apply into six balanced
+// base-256 digits in [-128, 128] (k_oz_digits).  Every D entry is the sum of
+// at most two psi entries with signs +-1 (one alpha source, one beta source:
+// every target string has at most one source under each pair operator), so
+// D's digit b is the signed sum of its sources' digits b, in [-256, 256]:
+// exact in BF16.  The slicer therefore only gathers digits and adds them (no
+// rounding, no per-determinant exponent).  Slices are stored as their true
+// values (digit * 2^{-8b}), so every product lands on one absolute scale and
+// the products are grouped by level L = a + b into four TMEM accumulators:
+// L = 2, 3 and 4 sum integers times 2^{-8L} that stay below 2^24 (exact in
+// FP32; level 4 can only exceed it for near-saturated digits); L = 5..7
+// share one accumulator whose FP32 rounding sits ~2^-48 below level 2.
+// Levels >= 8 are dropped: 20 BF16 products per tile (a <= 5, b <= 6).  The
+// error is absolute at ~2^-48 of the largest psi entry, i.e. norm-wise
+// relative ~1e-14 for a spread-out psi and ~1e-11 for one concentrated on a
+// few determinants (tests/test_ozaki_model.py models both).  The four
+// accumulators are combined into an FP32 pair (hi + lo, ~48 bits) and scaled
+// by 2^{eV(p) + g0 + 1}.
 //
-// Three kernels:
+// Kernels:
+//   k_oz_rowexp, k_oz_globalexp  g0 (and a flag for Inf/NaN input).
+//   k_oz_digits  the six digit planes of psi: [N] 16-byte words (digits 1-4,
+//               each a bf16x2 of the real and imaginary digit) and [N] 8-byte
+//               words (digits 5-6).
 //   k_oz_slice  one CTA per tile of 32 determinants (one alpha row): gathers
-//               D from a 62-bit fixed-point copy of psi through the per-pair
-//               target tables, finds each real column's exact exponent, cuts
-//               the values into the five BF16 slices and writes them to HBM
-//               already in the tensor core's shared-memory image (canonical
-//               no-swizzle K-major, 16-column K chunks, the two tiles of a
-//               tile pair interleaved chunk by chunk).
+//               the sources' digits through the per-pair target tables, adds
+//               them with their signs (bf16x2), and writes the six D slices
+//               to HBM already in the tensor core's shared-memory image
+//               (canonical no-swizzle K-major, 16-column K chunks, the two
+//               tiles of a tile pair interleaved chunk by chunk).
 //   k_oz_mma    persistent, one CTA per SM: a loader lane streams the slice
 //               images with cp.async.bulk into a ring of 16 KB slots (four K
 //               chunks of a tile pair each); the MMA warp runs the issue
@@ -38,10 +48,10 @@
 //               resident in shared memory); sixteen epilogue warps combine
 //               the four accumulators (single-buffered, 4 x NP TMEM columns)
 //               into G, stored coalesced as FP32 pairs [P][lena][w].
-//   k_oz_scatter  sigma from G in FP32-pair arithmetic (k_oz_rowexp,
-//               k_oz_globalexp and k_oz_fixed prepare the fixed-point psi).
+//   k_oz_scatter  sigma from G in FP32-pair arithmetic.
 // Every wait in k_oz_mma is bounded; on a timeout the kernel records an
-// error, lets the other roles leave, and frees its TMEM.
+// error, lets the other roles leave, waits for its issued copies and frees
+// its TMEM.
 #include <cuda_bf16.h>
 #include <math_constants.h>
 
@@ -55,7 +65,8 @@
 namespace fqegpu {
 
 namespace {
-constexpr int kSlices = 5;
+constexpr int kSlices = 5;     // slices of V
+constexpr int kDSlices = 6;    // slices (digits) of D
 constexpr int kMaxLevel = 7;   // pairs (a, b) with a + b <= 7 are contracted
 constexpr int kM = 128;        // MMA M (pairs, padded)
 constexpr int kN = 64;         // real columns of one slice tile
@@ -84,14 +95,14 @@ struct OzakiPlan {
   int64_t wb = 0;                      // beta columns per block (multiple of 32)
   __nv_bfloat16* d_vslices = nullptr;  // [npass][5][NP * KP] canonical K-major
   int32_t* d_vexp = nullptr;           // [npass * NP] row exponents
-  longlong2* d_psix = nullptr;         // [N]
+  uint4* d_pdA = nullptr;              // [N] digits 1-4 of psi (bf16x2 re, im each)
+  uint2* d_pdB = nullptr;              // [N] digits 5-6
   int32_t* d_rowexp = nullptr;         // [lena]
   int32_t* d_misc = nullptr;           // [0] = global exponent, [1] = error
   float4* d_G = nullptr;               // [P][lena][wb]
-  uchar2* d_bexp = nullptr;            // [N]
   int32_t* d_tabTA = nullptr;          // [lena][KP] target tables, pair index fastest
   int32_t* d_tabTB = nullptr;          // [lenb][KP]
-  __nv_bfloat16* d_dslices = nullptr;  // [tiles of a block][5][64 * KP] smem images
+  __nv_bfloat16* d_dslices = nullptr;  // [tiles of a block][6][64 * KP] smem images
   // beta-column blocks only: per block and target column, the pairs whose
   // beta source lies in the block, CSR: offsets [nblk][lenb + 1], entries
   // (pair, sign * (source - c0 + 1))
@@ -124,12 +135,12 @@ struct OzArgs {
   const int32_t* tabB;
   const int32_t* tabTA;  // [lena][KP]: the 8 pairs of an octet are 32 contiguous bytes
   const int32_t* tabTB;  // [lenb][KP]
-  const longlong2* psix;
+  const uint4* pdA;  // digit planes of psi (k_oz_digits)
+  const uint2* pdB;
   const int32_t* misc;
   const __nv_bfloat16* vslices;
   const int32_t* vexp;
-  uchar2* bexp;  // [N] bit length of max |D| (fixed point), re / im
-  __nv_bfloat16* dslices;  // [ntiles][5][64 * KP]
+  __nv_bfloat16* dslices;  // [ntiles][6][64 * KP]
   float4* G;
   int32_t* err;
   long long wait_cycles;  // limit of every bounded wait
@@ -193,82 +204,29 @@ __device__ __forceinline__ float scale2(float x, int e) {
   return (x * pow2f(e1)) * pow2f(e2);
 }
 
-// m * 2^-sh rounded to nearest, saturated to 40 bits (m < 2^63).
-__device__ __forceinline__ uint64_t round40(uint64_t m, int sh) {
-  uint64_t r;
-  if (sh > 0) {
-    r = sh >= 64 ? 0ull : ((m + (1ull << (sh - 1))) >> sh);
-  } else {
-    r = (-sh >= 40) ? 0ull : (m << (-sh));
-  }
-  const uint64_t cap = (1ull << 40) - 1ull;
-  return r > cap ? cap : r;
-}
-
-// D[q][det] (real and imaginary part) in 62-bit fixed point from the alpha
-// and beta target-table entries ca, cb of the pair q (0: no source).
-__device__ __forceinline__ void gather_d(const OzArgs& A, int32_t ca, int32_t cb, uint32_t ia,
-                                         uint32_t ib, uint32_t lenb, long long& re,
-                                         long long& im) {
-  re = 0;
-  im = 0;
-  if (ca) {
-    const longlong2 x = __ldg(A.psix + ((uint32_t)(abs(ca) - 1) * lenb + ib));
-    if (ca > 0) { re += x.x; im += x.y; } else { re -= x.x; im -= x.y; }
-  }
-  if (cb) {
-    const longlong2 x = __ldg(A.psix + (ia * lenb + (uint32_t)(abs(cb) - 1)));
-    if (cb > 0) { re += x.x; im += x.y; } else { re -= x.x; im -= x.y; }
-  }
-}
-
-// Inserts the five slice bytes of the 40-bit magnitude m (value j of 8) into
-// the packed words: word 2 (b - 1) + j / 4, byte j % 4 holds slice b.
-__device__ __forceinline__ void pack_slices(uint32_t (&pk)[2 * kSlices], uint64_t m, int j) {
-  const uint32_t lo = (uint32_t)m, hi = (uint32_t)(m >> 32);
-  const int h = j >> 2, pos = j & 3;
-  // selector: keep bytes of pk (0..3) except `pos`, which takes byte `src` of
-  // the second operand (4..7)
-  auto sel = [pos](int src) -> uint32_t {
-    uint32_t r = 0x3210u;
-    r &= ~(0xFu << (4 * pos));
-    r |= (uint32_t)(4 + src) << (4 * pos);
-    return r;
-  };
-  pk[0 + h] = __byte_perm(pk[0 + h], hi, sel(0));  // slice 1: bits 32..39
-  pk[2 + h] = __byte_perm(pk[2 + h], lo, sel(3));  // slice 2: bits 24..31
-  pk[4 + h] = __byte_perm(pk[4 + h], lo, sel(2));  // slice 3
-  pk[6 + h] = __byte_perm(pk[6 + h], lo, sel(1));  // slice 4
-  pk[8 + h] = __byte_perm(pk[8 + h], lo, sel(0));  // slice 5: bits 0..7
-}
-
-// Bytes k and k+1 of `w` as a bf16 pair, signs from bits 0 and 1 of `neg`,
-// each +-byte * 2^-8b (exact); `ebits` are the float bits of 2^(23 - 8b).
-__device__ __forceinline__ uint32_t bf16_bytes_pair(uint32_t w, int k, uint32_t neg,
-                                                    uint32_t ebits) {
-  const float off = __uint_as_float(ebits);
-  const float f0 = __uint_as_float(__byte_perm(w, ebits, 0x7650u + (uint32_t)k)) - off;
-  const float f1 = __uint_as_float(__byte_perm(w, ebits, 0x7650u + (uint32_t)k + 1u)) - off;
-  const __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
-  const uint32_t sgn = ((neg & 1u) << 15) | (((neg >> 1) & 1u) << 31);
-  return *reinterpret_cast<const uint32_t*>(&h) ^ sgn;
+// The digit planes of psi[src]: word k < 4 of `a` or word k - 4 of `b`
+// holds digit k + 1 as a bf16x2 (real, imaginary).
+__device__ __forceinline__ uint32_t digit_word(const uint4& a, const uint2& b, int k) {
+  return k == 0 ? a.x : k == 1 ? a.y : k == 2 ? a.z : k == 3 ? a.w : k == 4 ? b.x : b.y;
 }
 
 // ---- slicing: D tiles in the tensor core's shared-memory image ------------
-// One CTA (16 warps) per tile of 32 determinants.  Warp w owns determinants
+// One CTA (8 H warps) per tile of 32 determinants.  Warp w owns determinants
 // 4 (w % 8) .. 4 (w % 8) + 3 (MMA rows 8 (w % 8) .. + 7) and octets
 // 8 (w / 8) .. 8 (w / 8) + 7 of the pair index; lane l the determinant
-// 4 (w % 8) + (l & 3) and the octet 8 (w / 8) + (l >> 2).  Writes, per tile and
-// slice, the 64 x KP BF16 operand in the canonical K-major core-matrix layout
-// (a warp stores 1 KB contiguous per instruction pair) and the exact exponent
-// of every real column (shuffle maximum inside a warp, shared memory across
-// the two warps of a determinant group).
+// 4 (w % 8) + (l & 3) and the octet 8 (w / 8) + (l >> 2).  For each of the
+// octet's eight pairs the thread reads the digit planes of its (at most) two
+// sources, flips their signs and adds them (bf16x2, exact), then writes per
+// slice the 8 real and 8 imaginary values as one 32-byte store of the
+// canonical K-major image (rows 2d and 2d + 1 of a core matrix).
 template <int H>  // H groups of eight octets: KP <= 64 H
 __global__ void __launch_bounds__(256 * H, H == 2 ? 2 : 1) k_oz_slice(OzArgs A) {
-  __shared__ int red[8 * H][4];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int grp = w & 7, half = w >> 3;
   const int64_t t = blockIdx.x;
+  const int KP = A.KP, noct = KP / 8;
+  const int o = 8 * half + (lane >> 2);
+  if (o >= noct) return;
   int64_t ia64, ib064;
   tile_coords(A, t, ia64, ib064);
   const uint32_t lenb32 = (uint32_t)A.lenb;
@@ -276,15 +234,9 @@ __global__ void __launch_bounds__(256 * H, H == 2 ? 2 : 1) k_oz_slice(OzArgs A) 
   const int d = 4 * grp + (lane & 3);
   const uint32_t ib = (uint32_t)ib064 + d;
   const bool valid = ib < lenb32;
-  const int KP = A.KP, noct = KP / 8;
-  const int o = 8 * half + (lane >> 2);
-  const bool live = o < noct && valid;
-  uint64_t mre[8], mim[8];
-  uint32_t nre = 0u, nim = 0u;
-  int blr = 0, bli = 0;
   // the octet's eight table entries per spin: two 16-byte loads each
   int4 ta0 = make_int4(0, 0, 0, 0), ta1 = ta0, tb0 = ta0, tb1 = ta0;
-  if (live) {
+  if (valid) {
     const int4* pa = reinterpret_cast<const int4*>(A.tabTA + (size_t)ia * KP + 8 * o);
     const int4* pb = reinterpret_cast<const int4*>(A.tabTB + (size_t)ib * KP + 8 * o);
     ta0 = __ldg(pa);
@@ -294,67 +246,57 @@ __global__ void __launch_bounds__(256 * H, H == 2 ? 2 : 1) k_oz_slice(OzArgs A) 
   }
   const int32_t cas[8] = {ta0.x, ta0.y, ta0.z, ta0.w, ta1.x, ta1.y, ta1.z, ta1.w};
   const int32_t cbs[8] = {tb0.x, tb0.y, tb0.z, tb0.w, tb1.x, tb1.y, tb1.z, tb1.w};
+  // re[k][j / 2], im[k][j / 2]: slice k of pairs j (low half) and j + 1
+  uint32_t re[kDSlices][4], im[kDSlices][4];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    long long re, im;
-    gather_d(A, cas[j], cbs[j], ia, ib, lenb32, re, im);
-    nre |= (re < 0 ? 1u : 0u) << j;
-    nim |= (im < 0 ? 1u : 0u) << j;
-    mre[j] = (uint64_t)(re < 0 ? -re : re);
-    mim[j] = (uint64_t)(im < 0 ? -im : im);
-    blr = max(blr, 64 - __clzll((long long)mre[j]));
-    bli = max(bli, 64 - __clzll((long long)mim[j]));
+  for (int jp = 0; jp < 4; ++jp) {
+    uint32_t sum[2][kDSlices];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int j = 2 * jp + u;
+      const int32_t ca = cas[j], cb = cbs[j];
+      uint4 a4 = make_uint4(0u, 0u, 0u, 0u), b4 = a4;
+      uint2 a2 = make_uint2(0u, 0u), b2 = a2;
+      if (ca) {
+        const uint32_t idx = (uint32_t)(abs(ca) - 1) * lenb32 + ib;
+        a4 = __ldg(A.pdA + idx);
+        a2 = __ldg(A.pdB + idx);
+      }
+      if (cb) {
+        const uint32_t idx = ia * lenb32 + (uint32_t)(abs(cb) - 1);
+        b4 = __ldg(A.pdA + idx);
+        b2 = __ldg(A.pdB + idx);
+      }
+      // a negative table entry flips the sign of both halves
+      const uint32_t ma = ca < 0 ? 0x80008000u : 0u, mb = cb < 0 ? 0x80008000u : 0u;
+#pragma unroll
+      for (int k = 0; k < kDSlices; ++k) {
+        const uint32_t x = digit_word(a4, a2, k) ^ ma, y = digit_word(b4, b2, k) ^ mb;
+        const __nv_bfloat162 z = __hadd2(*reinterpret_cast<const __nv_bfloat162*>(&x),
+                                         *reinterpret_cast<const __nv_bfloat162*>(&y));
+        sum[u][k] = *reinterpret_cast<const uint32_t*>(&z);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kDSlices; ++k) {
+      re[k][jp] = __byte_perm(sum[0][k], sum[1][k], 0x5410u);  // the two real halves
+      im[k][jp] = __byte_perm(sum[0][k], sum[1][k], 0x7632u);  // the two imaginary halves
+    }
   }
-#pragma unroll
-  for (int m = 4; m < 32; m <<= 1) {
-    blr = max(blr, __shfl_xor_sync(0xffffffffu, blr, m));
-    bli = max(bli, __shfl_xor_sync(0xffffffffu, bli, m));
-  }
-  if (lane < 4) red[w][lane] = blr | (bli << 8);
-  __syncthreads();
-#pragma unroll
-  for (int h = 0; h < H; ++h) {
-    const int other = red[grp + 8 * h][lane & 3];
-    blr = max(blr, other & 0xFF);
-    bli = max(bli, other >> 8);
-  }
-  if (half == 0 && lane < 4 && valid)
-    A.bexp[ia * lenb32 + ib] = make_uchar2((unsigned char)blr, (unsigned char)bli);
-  uint32_t pk[2][2 * kSlices];
-#pragma unroll
-  for (int x = 0; x < 2 * kSlices; ++x) pk[0][x] = pk[1][x] = 0u;
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    pack_slices(pk[0], round40(mre[j], blr - 40), j);
-    pack_slices(pk[1], round40(mim[j], bli - 40), j);
-  }
-  if (o >= noct) return;
   // image of a tile pair: [slice][K chunk][tile of the pair][64 x 16 canonical
-  // K-major], so one K chunk of both tiles (4 KB) is the 128-row B operand
+  // K-major], so one K chunk of both tiles (4 KB) is the 128-row A operand
   const size_t chunk = (size_t)(KP / kChunkK) * kPairChunkElems;  // one slice
-  __nv_bfloat16* out = A.dslices + (size_t)(t >> 1) * kSlices * chunk;
+  __nv_bfloat16* out = A.dslices + (size_t)(t >> 1) * kDSlices * chunk;
   const uint32_t coff = (uint32_t)(o >> 1) * kPairChunkElems + (uint32_t)(t & 1) * kChunkElems;
 #pragma unroll
-  for (int b = 1; b <= kSlices; ++b) {
-    const uint32_t ebits = (uint32_t)(150 - 8 * b) << 23;
-    __nv_bfloat16* dst = out + (size_t)(b - 1) * chunk;
-    uint32_t v[2][4];
-#pragma unroll
-    for (int part = 0; part < 2; ++part) {
-      const uint32_t nb = part ? nim : nre;
-      const uint32_t lo = pk[part][2 * (b - 1)], hi = pk[part][2 * (b - 1) + 1];
-      v[part][0] = bf16_bytes_pair(lo, 0, nb, ebits);
-      v[part][1] = bf16_bytes_pair(lo, 2, nb >> 2, ebits);
-      v[part][2] = bf16_bytes_pair(hi, 0, nb >> 4, ebits);
-      v[part][3] = bf16_bytes_pair(hi, 2, nb >> 6, ebits);
-    }
+  for (int k = 0; k < kDSlices; ++k) {
     // rows 2d (real part) and 2d + 1 (imaginary part) are the two adjacent
     // 16-byte rows of one core matrix: one 32-byte store (2d is even, so the
     // address is 32-byte aligned)
-    __nv_bfloat16* q = dst + coff + tc::kmajor_offset(2 * d, 8 * (o & 1), kChunkK);
-    asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(q), "r"(v[0][0]),
-                 "r"(v[0][1]), "r"(v[0][2]), "r"(v[0][3]), "r"(v[1][0]), "r"(v[1][1]),
-                 "r"(v[1][2]), "r"(v[1][3])
+    __nv_bfloat16* q = out + (size_t)k * chunk + coff + tc::kmajor_offset(2 * d, 8 * (o & 1), kChunkK);
+    asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(q), "r"(re[k][0]),
+                 "r"(re[k][1]), "r"(re[k][2]), "r"(re[k][3]), "r"(im[k][0]), "r"(im[k][1]),
+                 "r"(im[k][2]), "r"(im[k][3])
                  : "memory");
   }
 }
@@ -436,8 +378,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       bool ok = true;
       for (int64_t t = t_begin; t < t_end && ok; ++t) {
         const __nv_bfloat16* src =
-            A.dslices + (size_t)t * kSlices * nch * kPairChunkElems;
-        for (int b = 0; b < kSlices && ok; ++b) {
+            A.dslices + (size_t)t * kDSlices * nch * kPairChunkElems;
+        for (int b = 0; b < kDSlices && ok; ++b) {
           for (int gi = 0; gi < ngr; ++gi) {
             const int c0 = gi * kGroupK;
             const uint32_t bytes = (uint32_t)min(kGroupK, nch - c0) * pchunk_bytes;
@@ -515,7 +457,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       // chunk group (b, gi): up to four 16-column K chunks of D slice b; a
       // slot is released as soon as its MMAs complete
 #pragma unroll
-      for (int b = 1; b <= kSlices; ++b) {
+      for (int b = 1; b <= kDSlices; ++b) {
         for (int gi = 0; gi < ngr && ok; ++gi) {
           const int c0 = gi * kGroupK;
           const int nk = min(kGroupK, nch - c0);
@@ -576,7 +518,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
     const int part = row & 1;                 // 0 real, 1 imaginary
     const int cw = NP / 4;                    // pairs per column group
     const int pbeg = cg * cw;
-    const int g0 = A.misc[0];
+    // D = 2^(g0 + 1) sum_b slice_b for every determinant (one global scale)
+    const int colexp = A.misc[0] + 1;
     int64_t it = 0;
     for (int64_t t = t_begin; t < t_end; ++t, ++it) {
       const int64_t ts = 2 * t + half;
@@ -585,11 +528,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       if (live_tile) tile_coords(A, ts, ia, ib0);
       const int64_t ib = ib0 + det;
       const bool live = live_tile && ib < A.lenb;
-      int bits = 0;
-      if (live) {
-        const uchar2 be = A.bexp[ia * A.lenb + ib];
-        bits = part ? be.y : be.x;
-      }
       const bool got = __all_sync(0xffffffffu,
                                   oz_wait(accfull, (uint32_t)(it & 1), abort_flag, A.wait_cycles));
       if (!got) {
@@ -603,7 +541,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       // then levels 4 and 5..7), scaled, and held in registers; the
       // accumulators are released before the G stores, so the next tile
       // pair's MMAs run while this one's G goes out
-      const int colexp = bits - 62 + g0;  // |D| < 2^colexp in this column
       float hreg[kM / 4], lreg[kM / 4];
 #pragma unroll
       for (int c0 = 0; c0 < kM / 4; c0 += 4) {
@@ -709,21 +646,48 @@ __global__ void k_oz_globalexp(int64_t lena, const int32_t* __restrict__ rowexp,
   }
 }
 
-// psix = round(psi * 2^(62 - g0)), |psix| < 2^62.
-__global__ void k_oz_fixed(int64_t n, const double2* __restrict__ psi,
-                           const int32_t* __restrict__ misc,
-                           longlong2* __restrict__ psix) {
+// The six balanced base-256 digits of x = round(v 2^(47 - g0)), |x| <= 2^47:
+// digit b (b = 1..5) = floor(r / 2^k + 1/2) with k = 8 (6 - b) and r the
+// remainder so far (|r| <= 128 2^k, so the digit lies in [-128, 128]); the
+// last digit is the final remainder.  Returned as floats digit * 2^-8b.
+__device__ __forceinline__ void psi_digits(long long x, float (&f)[kDSlices]) {
+#pragma unroll
+  for (int b = 1; b < kDSlices; ++b) {
+    const int k = 8 * (kDSlices - b);
+    const long long dgt = (x + (1ll << (k - 1))) >> k;
+    x -= dgt << k;
+    f[b - 1] = (float)dgt * __int_as_float((127 - 8 * b) << 23);
+  }
+  f[kDSlices - 1] = (float)x * __int_as_float((127 - 8 * kDSlices) << 23);
+}
+
+// The digit planes of psi at the global exponent g0: pdA[i] = digits 1-4,
+// pdB[i] = digits 5-6, each digit a bf16x2 (real, imaginary); exact.
+__global__ void k_oz_digits(int64_t n, const double2* __restrict__ psi,
+                            const int32_t* __restrict__ misc, uint4* __restrict__ pdA,
+                            uint2* __restrict__ pdB) {
   const int g0 = misc[0];
   const bool skip = misc[2] != 0;  // non-finite input: the output is NaN anyway
+  // 2^(47 - g0) in two factors, each within double range for any finite psi
+  const int e = 47 - g0, e1 = e / 2, e2 = e - e1;
+  const double s1 = __longlong_as_double((long long)(1023 + e1) << 52);
+  const double s2 = __longlong_as_double((long long)(1023 + e2) << 52);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    longlong2 o = make_longlong2(0, 0);
-    if (g0 > kExpZero && !skip) {
+    float fr[kDSlices] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, fi[kDSlices] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (!skip) {
       const double2 v = psi[i];
-      o.x = __double2ll_rn(ldexp(v.x, 62 - g0));
-      o.y = __double2ll_rn(ldexp(v.y, 62 - g0));
+      psi_digits(__double2ll_rn((v.x * s1) * s2), fr);
+      psi_digits(__double2ll_rn((v.y * s1) * s2), fi);
     }
-    psix[i] = o;
+    uint32_t wd[kDSlices];
+#pragma unroll
+    for (int k = 0; k < kDSlices; ++k) {
+      const __nv_bfloat162 h = __floats2bfloat162_rn(fr[k], fi[k]);  // exact
+      wd[k] = *reinterpret_cast<const uint32_t*>(&h);
+    }
+    pdA[i] = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+    pdB[i] = make_uint2(wd[4], wd[5]);
   }
 }
 
@@ -930,9 +894,10 @@ static int plan_create(fqegpu_ham h) {
   FQE_CUDA(cudaMemcpy(pl->d_vexp, vexp.data(), sizeof(int32_t) * vexp.size(),
                       cudaMemcpyHostToDevice));
   const int64_t lena = h->g->a.len, lenb = h->g->b.len, N = lena * lenb;
-  // beta-column blocks: slice images (20 KP bytes) and G (16 P bytes) per
-  // determinant of a block within the handle's scratch limit
-  const int64_t per_col = (int64_t)(20 * KP + 16 * P) * lena;
+  // beta-column blocks: slice images (24 KP bytes: six BF16 slices of the
+  // real and imaginary part) and G (16 P bytes) per determinant of a block
+  // within the handle's scratch limit
+  const int64_t per_col = (int64_t)(2 * 2 * kDSlices * KP + 16 * P) * lena;
   int64_t wb = h->scratch_limit / std::max<int64_t>(per_col, 1);
   if (wb >= lenb) {
     wb = lenb;  // one block: G is [P][lena][lenb]
@@ -940,7 +905,8 @@ static int plan_create(fqegpu_ham h) {
     wb = std::max<int64_t>(kDets, wb / kDets * kDets);
   }
   pl->wb = wb;
-  FQE_CUDA(dev_alloc(&pl->d_psix, sizeof(longlong2) * N));
+  FQE_CUDA(dev_alloc(&pl->d_pdA, sizeof(uint4) * N));
+  FQE_CUDA(dev_alloc(&pl->d_pdB, sizeof(uint2) * N));
   FQE_CUDA(dev_alloc(&pl->d_rowexp, sizeof(int32_t) * lena));
   FQE_CUDA(dev_alloc(&pl->d_misc, sizeof(int32_t) * 4));
   FQE_CUDA(cudaMemset(pl->d_misc, 0, sizeof(int32_t) * 4));
@@ -948,11 +914,9 @@ static int plan_create(fqegpu_ham h) {
   *pl->h_err = 0;
   FQE_CUDA(cudaEventCreateWithFlags(&pl->err_ev, cudaEventDisableTiming));
   FQE_CUDA(dev_alloc(&pl->d_G, sizeof(float4) * (size_t)P * lena * wb));
-  FQE_CUDA(dev_alloc(&pl->d_bexp, sizeof(uchar2) * N));
   {
-    const bool tri = h->compressed;
-    const int32_t* ta = tri ? h->g->a.tab_tri : h->g->a.tab_full;
-    const int32_t* tb = tri ? h->g->b.tab_tri : h->g->b.tab_full;
+    const int32_t* ta = ham_tabA(h);
+    const int32_t* tb = ham_tabB(h);
     FQE_CUDA(dev_alloc(&pl->d_tabTA, sizeof(int32_t) * (size_t)lena * KP));
     FQE_CUDA(dev_alloc(&pl->d_tabTB, sizeof(int32_t) * (size_t)lenb * KP));
     k_oz_transpose_tab<<<(unsigned)((lena * KP + 255) / 256), 256>>>(P, KP, lena, ta,
@@ -965,8 +929,7 @@ static int plan_create(fqegpu_ham h) {
   if (wb < lenb) {
     // per block, for every target column, the (pair, source) entries whose
     // beta source lies in the block, in pair order
-    const bool tri = h->compressed;
-    const int32_t* tb = tri ? h->g->b.tab_tri : h->g->b.tab_full;
+    const int32_t* tb = ham_tabB(h);
     std::vector<int32_t> tab((size_t)P * lenb);
     FQE_CUDA(cudaMemcpy(tab.data(), tb, sizeof(int32_t) * tab.size(), cudaMemcpyDeviceToHost));
     const int64_t nblk = (lenb + wb - 1) / wb;
@@ -999,7 +962,7 @@ static int plan_create(fqegpu_ham h) {
   }
   const int64_t ntiles = lena * ((wb + kDets - 1) / kDets);  // tiles of the widest block
   const int64_t npairs = (ntiles + 1) / 2;
-  const size_t dsl = sizeof(__nv_bfloat16) * (size_t)npairs * 2 * kSlices * kN * KP;
+  const size_t dsl = sizeof(__nv_bfloat16) * (size_t)npairs * 2 * kDSlices * kN * KP;
   FQE_CUDA(dev_alloc(&pl->d_dslices, dsl));
   FQE_CUDA(cudaMemset(pl->d_dslices, 0, dsl));  // an unpaired last tile reads zeros
   FQE_CUDA(cudaDeviceGetAttribute(&pl->nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -1072,11 +1035,11 @@ void ozaki_destroy(fqegpu_ham h) {
   if (!pl) return;
   cudaFree(pl->d_vslices);
   cudaFree(pl->d_vexp);
-  cudaFree(pl->d_psix);
+  cudaFree(pl->d_pdA);
+  cudaFree(pl->d_pdB);
   cudaFree(pl->d_rowexp);
   cudaFree(pl->d_misc);
   cudaFree(pl->d_G);
-  cudaFree(pl->d_bexp);
   cudaFree(pl->d_tabTA);
   cudaFree(pl->d_tabTB);
   cudaFree(pl->d_dslices);
@@ -1108,14 +1071,13 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   }
   OzakiPlan* pl = h->oz;
   if (!h->defer_check) FQE_TRY(ozaki_poll(pl, st));
-  const bool tri = h->compressed;
-  const int32_t* tabA = tri ? g->a.tab_tri : g->a.tab_full;
-  const int32_t* tabB = tri ? g->b.tab_tri : g->b.tab_full;
+  const int32_t* tabA = ham_tabA(h);
+  const int32_t* tabB = ham_tabB(h);
   h->events_used = 0;
   FQE_TRY(stage_mark(h, 0, 0, st));
   k_oz_rowexp<<<(unsigned)lena, 256, 0, st>>>(lenb, psi, pl->d_rowexp);
   k_oz_globalexp<<<1, 256, 0, st>>>(lena, pl->d_rowexp, pl->d_misc);
-  k_oz_fixed<<<kNumSMs * 8, 256, 0, st>>>(N, psi, pl->d_misc, pl->d_psix);
+  k_oz_digits<<<kNumSMs * 8, 256, 0, st>>>(N, psi, pl->d_misc, pl->d_pdA, pl->d_pdB);
   FQE_CUDA(cudaGetLastError());
   OzArgs A;
   A.P = pl->P;
@@ -1127,10 +1089,10 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   A.gld = pl->wb;
   A.tabA = tabA;
   A.tabB = tabB;
-  A.psix = pl->d_psix;
+  A.pdA = pl->d_pdA;
+  A.pdB = pl->d_pdB;
   A.misc = pl->d_misc;
   A.G = pl->d_G;
-  A.bexp = pl->d_bexp;
   A.tabTA = pl->d_tabTA;
   A.tabTB = pl->d_tabTB;
   A.dslices = pl->d_dslices;

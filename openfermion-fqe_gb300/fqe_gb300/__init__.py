@@ -10,7 +10,7 @@ All arithmetic runs in libfqegpu.so (hand-written sm_103a CUDA).
 from . import settings
 from .fci_graph import FciGraph
 from .fqe_data import FqeData
-from .hamiltonians import (DiagonalCoulomb, Hamiltonian, RestrictedHamiltonian,
+from .hamiltonians import (DiagonalCoulomb, General, Hamiltonian, RestrictedHamiltonian,
                            build_hamiltonian)
 from .util import alpha_beta_electrons, vdot
 from .wavefunction import Wavefunction

@@ -42,6 +42,7 @@ _SIGNATURES = {
     "fqegpu_graph_map_lengths": [_P, _I, _P],
     "fqegpu_graph_maps": [_P, _I, _P],
     "fqegpu_ham_create": [_P, _P, _P, _P, ctypes.POINTER(_P)],
+    "fqegpu_ham_create_spin": [_P, _P, _P, _P, ctypes.POINTER(_P)],
     "fqegpu_ham_destroy": [_P],
     "fqegpu_ham_info": [_P, _P],
     "fqegpu_ham_set_scratch_limit": [_P, _L],

@@ -35,15 +35,18 @@ def _host_c128(a) -> numpy.ndarray:
 
 
 class _Ham:
-    """Owner of one fqegpu_ham handle."""
+    """Owner of one fqegpu_ham handle: a restricted operator (h1 [n, n],
+    h2 [n]^4) or, with spin=True, a spin-orbital one (h1 [2n, 2n], h2
+    [2n]^4, alpha orbitals first)."""
 
-    def __init__(self, graph: FciGraph, h1, h2):
+    def __init__(self, graph: FciGraph, h1, h2, spin: bool = False):
         self.graph = graph  # keeps the graph alive as long as the handle
+        self.spin = spin
         self._h1 = None if h1 is None else _host_c128(h1)
         self._h2 = None if h2 is None else _host_c128(h2)
         h = ctypes.c_void_p()
         _lib.call(
-            "fqegpu_ham_create", graph.handle,
+            "fqegpu_ham_create_spin" if spin else "fqegpu_ham_create", graph.handle,
             None if self._h1 is None else self._h1.ctypes.data_as(
                 ctypes.c_void_p),
             None if self._h2 is None else self._h2.ctypes.data_as(
@@ -76,13 +79,13 @@ def _digest(a) -> Optional[bytes]:
         str(a.shape), "ascii")
 
 
-def ham_for(graph: FciGraph, h1, h2) -> _Ham:
+def ham_for(graph: FciGraph, h1, h2, spin: bool = False) -> _Ham:
     """Prepared Hamiltonian for a sector, cached on the tensors' contents."""
-    key = (graph.nalpha(), graph.nbeta(), graph.norb(), _digest(h1),
+    key = (graph.nalpha(), graph.nbeta(), graph.norb(), spin, _digest(h1),
            _digest(h2))
     ham = _HAM_CACHE.get(key)
     if ham is None:
-        ham = _Ham(graph, h1, h2)
+        ham = _Ham(graph, h1, h2, spin)
         _HAM_CACHE[key] = ham
         while len(_HAM_CACHE) > _HAM_CACHE_SIZE:
             _HAM_CACHE.popitem(last=False)
@@ -259,13 +262,18 @@ class FqeData:
         if not spatial and first.shape[0] != 2 * self.norb():
             raise ValueError("Inconsistent number of spin-orbitals in "
                              "operators and wavefunction.")
-        if not spatial or len_arr > 2:
+        if len_arr > 2:
             raise NotImplementedError(
-                "only spatial one- and two-body operators are on this path")
-        if len_arr == 1:
-            self.coeff = self._apply_array_spatial1(array[0])
+                "only one- and two-body operators are on this path")
+        if spatial:
+            if len_arr == 1:
+                self.coeff = self._apply_array_spatial1(array[0])
+            else:
+                self.coeff = self._apply_array_spatial12(array[0], array[1])
+        elif len_arr == 1:
+            self.coeff = self._apply_array_spin1(array[0])
         else:
-            self.coeff = self._apply_array_spatial12(array[0], array[1])
+            self.coeff = self._apply_array_spin12(array[0], array[1])
 
     def _run_apply(self, ham: _Ham, alpha=1.0, beta=0.0,
                    out: Optional[torch.Tensor] = None) -> torch.Tensor:
@@ -291,6 +299,22 @@ class FqeData:
         assert h1e.shape == (norb, norb)
         assert h2e.shape == (norb, norb, norb, norb)
         return self._run_apply(ham_for(self._core, h1e, h2e))
+
+    def _apply_array_spin1(self, h1e: numpy.ndarray) -> torch.Tensor:
+        """fqe_data.py:533-563: the alpha block of h1e on alpha strings, the
+        beta block on beta strings (fqegpu_ham_create_spin, one-body)."""
+        norb = self.norb()
+        assert h1e.shape == (norb * 2, norb * 2)
+        return self._run_apply(ham_for(self._core, h1e, None, spin=True))
+
+    def _apply_array_spin12(self, h1e: numpy.ndarray,
+                            h2e: numpy.ndarray) -> torch.Tensor:
+        """fqe_data.py:614-635, 743-773: spin-orbital one- and two-body
+        operators (fqegpu_ham_create_spin)."""
+        norb = self.norb()
+        assert h1e.shape == (norb * 2, norb * 2)
+        assert h2e.shape == (norb * 2, norb * 2, norb * 2, norb * 2)
+        return self._run_apply(ham_for(self._core, h1e, h2e, spin=True))
 
     # -- diagonal Coulomb (fqe_data.py:263-402) ------------------------------
     def _diag_coulomb(self, diag, array, inplace: bool, mode: int):

@@ -5,23 +5,26 @@ contraction G = V D of this project's apply, for checking its numerical
 design on the CPU.  The reference has no counterpart: it contracts in FP64
 (lib/fqe_data.c:879-970); the FP64 result here is the exact reference value.
 
-What is modelled (csrc/ozaki.cu, k_oz_slice / k_oz_mma):
+What is modelled (csrc/ozaki.cu, k_oz_digits / k_oz_slice / k_oz_mma):
 
-* each real column of D (one determinant, real or imaginary part, all pair
-  rows) is scaled by its exact exponent e (max |D| < 2^e) and rounded to a
-  40-bit magnitude; each row of V likewise with its row exponent;
-* a 40-bit magnitude m is cut into five bytes; slice k holds
-  sign * byte_k * 2^-8k, exactly representable in BF16;
-* the 19 products (a, b) with a + b <= 7 (a: V slice, b: D slice) are summed
-  per K step of 16 pairs into four FP32 accumulators: levels 2, 3, 4 alone
-  (integer sums below 2^24 at one scale: exact) and levels 5..7 together;
+* each row of V is scaled by its exponent e (max |V| < 2^e), rounded to a
+  40-bit magnitude and cut into five bytes; slice a holds
+  sign * byte_a * 2^-8a, exactly representable in BF16;
+* psi is scaled by one global exponent g0 to a 47-bit integer and cut into
+  six balanced base-256 digits in [-128, 128]; D's digit b is the signed sum
+  of its (at most two) sources' digits b, in [-256, 256], exact in BF16
+  (`psi_digit_slices`, `contract_psi_digits`);
+* the 20 products (a, b) with a + b <= 7 (a <= 5: V slice, b <= 6: D slice)
+  are summed per K step of 16 pairs into four FP32 accumulators: levels 2,
+  3, 4 alone (integer sums below 2^24 at one scale: exact) and levels 5..7
+  together;
 * the four level sums are combined by an exact two-sum of levels 2 and 3,
-  the low part adding levels 4 and 5..7, and scaled by 2^(e_row + e_col).
+  the low part adding levels 4 and 5..7, and scaled by 2^(e_row + g0 + 1).
 
-The determinant-side exponents here come straight from D (the kernel
-derives them from a 62-bit fixed-point copy of psi, which adds at most
-2^-62 relative); the FP32-pair scatter that follows on the device adds about
-2^-48 relative and is not modelled.
+`contract` models the form the kernel had before: D's columns scaled by
+their exact exponents and rounded to 40-bit magnitudes (five slices, 19
+products); it is kept to compare the two designs.  The FP32-pair scatter
+that follows on the device adds about 2^-48 relative and is not modelled.
 """
 
 import numpy
@@ -112,6 +115,87 @@ def contract(V, D, e_det=None):
     acc, e_row, e_col = level_sums(V, Dr, e_col=e_col)
     G = combine(acc, e_row, e_col)
     n = D.shape[1]
+    return G[:, :n] + 1j * G[:, n:]
+
+
+# ---- the gather-free slicing: psi cut once into digits -----------------------
+# csrc/ozaki.cu, k_oz_digits / k_oz_slice: psi is scaled by one global
+# exponent g0 (max |Re|, |Im| < 2^g0) to a 47-bit fixed-point integer and cut
+# into six balanced base-256 digits in [-128, 128] (the last digit exact),
+# stored as digit * 2^-8b; a D entry is a sum of at most two psi entries with
+# signs +-1 (one alpha and one beta source), so its digit b is the sum of the
+# sources' digits b, in [-256, 256]: exact in BF16, with no rounding and no
+# per-column exponent.  D = 2^(g0+1) sum_b slice_b.  The 20 products a + b <= 7
+# (a <= 5 slices of V, b <= 6 of D) reach 2^-48 of the global scale.
+
+PSI_DIGITS = 6
+
+
+def psi_digit_slices(psi):
+    """(slices, g0): slices[b - 1] = digit_b(Re psi) 2^-8b + i digit_b(Im psi)
+    2^-8b for b = 1..6, and the global exponent g0."""
+    mx = max(numpy.abs(psi.real).max(), numpy.abs(psi.imag).max())
+    g0 = int(numpy.frexp(mx)[1]) if mx > 0 else 0
+    out = []
+    parts = []
+    for comp in (psi.real, psi.imag):
+        x = numpy.rint(numpy.ldexp(comp, 47 - g0)).astype(numpy.int64)
+        digs = []
+        for b in range(1, PSI_DIGITS):
+            k = 8 * (PSI_DIGITS - b)
+            d = (x + (1 << (k - 1))) >> k
+            x = x - (d << k)
+            digs.append(d)
+        digs.append(x)  # the last digit is the remainder, |x| <= 128
+        parts.append(digs)
+    for b in range(PSI_DIGITS):
+        for d in (parts[0][b], parts[1][b]):
+            assert numpy.abs(d).max() <= 128
+        out.append((parts[0][b] + 1j * parts[1][b]) * 2.0 ** (-8 * (b + 1)))
+    return out, g0
+
+
+def digit_level_sums(vs, ds, fp32=True):
+    """The four level accumulators [4, P, M] of sum_ab vs[a] ds[b] (a + b <=
+    MAX_LEVEL) in K steps of 16; float64 accumulation with fp32=False."""
+    dt = numpy.float32 if fp32 else numpy.float64
+    P, K = vs[0].shape
+    acc = numpy.zeros((4, P, ds[0].shape[1]), dtype=dt)
+    for b in range(1, len(ds) + 1):
+        for a in range(1, min(len(vs), MAX_LEVEL - b) + 1):
+            lvl = a + b
+            ai = lvl - 2 if lvl <= 4 else 3
+            for k0 in range(0, K, KSTEP):
+                part = vs[a - 1][:, k0:k0 + KSTEP] @ ds[b - 1][k0:k0 + KSTEP, :]
+                acc[ai] = (acc[ai].astype(numpy.float64) + part).astype(dt)
+    return acc
+
+
+def digit_slices_of_dvec(psi, dvec):
+    """D's six slices (real and imaginary columns side by side) from psi's
+    digit planes through the gather dvec, and g0."""
+    dslices, g0 = psi_digit_slices(psi)
+    ds = []
+    for b, sl in enumerate(dslices, 1):
+        D = dvec(sl)
+        Dr = numpy.concatenate([D.real, D.imag], axis=1)
+        assert numpy.abs(Dr * 2.0 ** (8 * b)).max() <= 256
+        ds.append(Dr)
+    return ds, g0
+
+
+def contract_psi_digits(V, psi, dvec, fp32=True):
+    """The modelled tensor-core G = V D with D's slices formed from psi's
+    digits: dvec(x) is the (linear, +-1) gather D = E x of the apply, applied
+    to each digit plane; returns G [P, N] complex."""
+    ds, g0 = digit_slices_of_dvec(psi, dvec)
+    e_row = _exponents(V, 1)
+    vs = slices(V, e_row[:, None])
+    acc = digit_level_sums(vs, ds, fp32=fp32)
+    M = ds[0].shape[1]
+    e_col = numpy.full(M, g0 + 1)
+    G = combine(acc, e_row, e_col)
+    n = M // 2
     return G[:, :n] + 1j * G[:, n:]
 
 

@@ -1,10 +1,14 @@
 """The numerical design of the tensor-core (Ozaki-split BF16) contraction,
-checked on the CPU with the numpy model oracle/ozaki_model.py (five 8-bit
-slices of 40-bit fixed point per operand, 19 products a + b <= 7, four FP32
-level accumulators, two-sum combination): the level sums 2-4 are exact, and
-the contraction and the apply stay within the 1e-10 relative bound the GPU
-tests hold the kernel to.  The same design's device results are compared
-with the oracle in tests/test_gpu_ozaki.py."""
+checked on the CPU with the numpy model oracle/ozaki_model.py: V in five
+8-bit slices of 40-bit fixed point per row, psi cut once into six balanced
+8-bit digits at one global exponent (D's digits are exact sums of two
+sources' digits), 20 products a + b <= 7, four FP32 level accumulators,
+two-sum combination.  The level sums 2-4 are exact, and the contraction and
+the apply stay within the 1e-10 relative bound the GPU tests hold the kernel
+to, for spread-out and for concentrated psi.  The earlier per-column form
+(exact column exponents, five D slices) is compared alongside.  The same
+design's device results are compared with the oracle in
+tests/test_gpu_ozaki.py."""
 
 import numpy
 import pytest
@@ -28,6 +32,55 @@ def _case(oracle, norb, na, nb, seed, peaked=False):
     assert numpy.abs(V.imag).max() == 0.0  # real integrals: the tensor-core form
     D = oracle.make_dvec(psi, g).reshape(norb * norb, -1)
     return h1, h2, psi, g, V.real.copy(), D
+
+
+def _dvec(oracle, g, norb):
+    return lambda x: oracle.make_dvec(x, g).reshape(norb * norb, -1)
+
+
+def test_psi_digits_reconstruct_psi():
+    import ozaki_model as om
+    rng = numpy.random.default_rng(2)
+    psi = rng.normal(size=(40, 30)) + 1j * rng.normal(size=(40, 30))
+    psi[3, 4] = 7.5 - 0.25j
+    sl, g0 = om.psi_digit_slices(psi)
+    back = 2.0 ** (g0 + 1) * sum(sl)
+    # 47-bit fixed point at the global scale: |error| <= 2^(g0 - 48) in the
+    # real and in the imaginary part
+    assert numpy.abs((back - psi).real).max() <= 2.0 ** (g0 - 48)
+    assert numpy.abs((back - psi).imag).max() <= 2.0 ** (g0 - 48)
+    for b, x in enumerate(sl, 1):
+        for part in (x.real, x.imag):
+            d = part * 2.0 ** (8 * b)
+            assert numpy.array_equal(d, numpy.round(d))  # integers
+            assert numpy.abs(d).max() <= 128
+
+
+def test_digit_levels_2_to_4_are_exact(oracle):
+    import ozaki_model as om
+    *_, g, V, _ = _case(oracle, 8, 4, 4, 3)
+    _, _, psi = __import__("fqe_gb300.synthetic", fromlist=["x"]).sector(8, 4, 4, 16, 3)
+    ds, _ = om.digit_slices_of_dvec(psi, _dvec(oracle, g, 8))
+    vs = om.slices(V, om._exponents(V, 1)[:, None])
+    a32 = om.digit_level_sums(vs, ds, fp32=True)
+    a64 = om.digit_level_sums(vs, ds, fp32=False)
+    for lvl in range(3):  # levels 2, 3, 4
+        assert numpy.array_equal(a32[lvl].astype(numpy.float64), a64[lvl])
+    assert numpy.abs(a32[3] - a64[3]).max() <= 2.0 ** -40 * numpy.abs(a64[0]).max()
+
+
+@pytest.mark.parametrize("norb,na,nb,peaked", [(8, 4, 4, False), (8, 3, 5, False),
+                                               (10, 5, 5, False), (8, 4, 4, True),
+                                               (10, 5, 5, True)])
+def test_digit_contraction_and_apply_within_bound(oracle, norb, na, nb, peaked):
+    import ozaki_model as om
+    h1, h2, psi, g, V, D = _case(oracle, norb, na, nb, norb + na, peaked)
+    G = om.contract_psi_digits(V, psi, _dvec(oracle, g, norb))
+    assert _rel(G, V @ D) < 3e-11  # measured 3e-12 (spread) to 1e-11 (peaked)
+    shape = (norb, norb, g.lena, g.lenb)
+    ref = oracle.apply_spatial12(psi, h1, h2, g)
+    # measured 2.4e-12 to 7.7e-12: well inside the 1e-10 bound
+    assert _rel(oracle.make_coeff(G.reshape(shape), g), ref) < 2e-11
 
 
 def test_levels_2_to_4_are_exact(oracle):
@@ -87,3 +140,19 @@ def test_fewer_slices_would_break_the_bound(oracle):
     finally:
         om.MAX_LEVEL = old
     assert _rel(G5, V @ Dr) > 1e-9
+
+
+def test_digit_form_needs_level_7(oracle):
+    # with psi's digits at one global exponent, dropping level 7 (15 instead
+    # of 20 products) leaves psi effectively 40-bit at the global scale: too
+    # coarse for a concentrated psi
+    import ozaki_model as om
+    h1, h2, psi, g, V, D = _case(oracle, 10, 5, 5, 15, True)
+    old = om.MAX_LEVEL
+    try:
+        om.MAX_LEVEL = 6
+        G6 = om.contract_psi_digits(V, psi, _dvec(oracle, g, 10))
+    finally:
+        om.MAX_LEVEL = old
+    G7 = om.contract_psi_digits(V, psi, _dvec(oracle, g, 10))
+    assert _rel(G6, V @ D) > 5 * _rel(G7, V @ D)
