@@ -262,6 +262,27 @@ int fqegpu_batch_taylor_create(int n, const fqegpu_ham *hams,
                                void *stream, fqegpu_batch *out);
 int fqegpu_batch_taylor_terms(fqegpu_batch b, int *h_terms, void *stream);
 
+/* ---- orbital rotation and diagonal evolution --------------------------------
+ * d_psi <- (prod over icol of X^beta_icol(m_b)) (prod over icol of
+ * X^alpha_icol(m_a)) d_psi, columns in ascending order, alpha first, with the
+ * column operator X_icol(m) = 1 + sum_i m[i][icol] E_{i,icol} on the strings
+ * of one spin: FqeData.apply_columns_recursive_inplace (fqe_data.py:1510-1535)
+ * and lm_apply_array1_column_alpha (lib/fqe_data.c:305-347), the kernel of
+ * Wavefunction.transform (wavefunction.py:813-959).  h_mat_a, h_mat_b:
+ * complex128 [norb][norb] on the host (the host side forms them from the LU
+ * factors of the rotation); d_work: a device array of the sector's size,
+ * overwritten (each column is one pass from one array into the other; the
+ * result ends in d_psi).  norb <= 64, at most 65535 strings per spin. */
+int fqegpu_transform(fqegpu_graph g, const double *h_mat_a,
+                     const double *h_mat_b, double *d_psi, double *d_work,
+                     void *stream);
+/* d_psi[a][b] *= exp(sum_{i in a} h_diag_a[i] + sum_{j in b} h_diag_b[j])
+ * (complex128 [norb] each, already multiplied by -i t):
+ * FqeData.evolve_diagonal (fqe_data.py:203-262). */
+int fqegpu_evolve_diagonal(fqegpu_graph g, const double *h_diag_a,
+                           const double *h_diag_b, double *d_psi,
+                           void *stream);
+
 /* ---- one-particle RDM -------------------------------------------------------
  * h_rdm[i][j] = <bra| E_ij |ket>, E_ij = sum over spin of a+_i a_j, complex128
  * [norb][norb] on the host: FqeData.rdm1(bradata) with ket = self and bra =

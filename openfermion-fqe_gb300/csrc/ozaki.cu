@@ -23,11 +23,13 @@
 // FP32; level 4 can only exceed it for near-saturated digits); L = 5..7
 // share one accumulator whose FP32 rounding sits ~2^-48 below level 2.
 // Levels >= 8 are dropped: 20 BF16 products per tile (a <= 5, b <= 6).  The
-// error is absolute at ~2^-48 of the largest psi entry, i.e. norm-wise
-// relative ~1e-14 for a spread-out psi and ~1e-11 for one concentrated on a
-// few determinants (tests/test_ozaki_model.py models both).  The four
-// accumulators are combined into an FP32 pair (hi + lo, ~48 bits) and scaled
-// by 2^{eV(p) + g0 + 1}.
+// four accumulators are combined by a chain of exact two-sums into an FP32
+// pair (hi + lo, ~48 bits; no level is assumed to hold the leading bits,
+// since at one global scale a small column starts in level 4 or later) and
+// scaled by 2^{eV(p) + g0 + 1}.  Modelled error on sigma (numpy model,
+// tests/test_ozaki_model.py): ~1e-12 for a spread-out psi, 2-3e-12 for one
+// concentrated on a few determinants, ~5e-13 for the high-order terms of a
+// Taylor series, against 1.7-4.6e-12 for exact per-determinant exponents.
 //
 // Kernels:
 //   k_oz_rowexp, k_oz_globalexp  g0 (and a flag for Inf/NaN input).
@@ -188,6 +190,13 @@ __device__ __forceinline__ bool oz_wait_drain(uint64_t* bar, uint32_t parity, lo
 __device__ __forceinline__ void oz_abort(volatile int* abort_flag, int32_t* err, int code) {
   *abort_flag = 1;
   atomicExch(err, code);
+}
+
+// s + e = a + b exactly (Knuth's two-sum, FP32).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
 }
 
 // 2^e as a float for -126 <= e <= 127.
@@ -554,12 +563,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
           tc::tmem_wait_ld();
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            const float x = __uint_as_float(ra[k]), y = __uint_as_float(rb[k]);
-            const float h = x + y;
-            const float bb = h - x;
-            float l = (x - (h - bb)) + (y - bb);
-            l += __uint_as_float(rc[k]);
-            l += __uint_as_float(rd[k]);
+            // a chain of exact two-sums: with one global scale a column's
+            // leading bits may sit in level 4 or later, so no level is
+            // assumed to dominate; the rounding errors are summed in l
+            float h, l;
+            two_sum(__uint_as_float(ra[k]), __uint_as_float(rb[k]), h, l);
+            float e2;
+            two_sum(h, __uint_as_float(rc[k]), h, e2);
+            l += e2;
+            two_sum(h, __uint_as_float(rd[k]), h, e2);
+            l += e2;
             const float h2 = h + l;
             const float l2 = l - (h2 - h);
             // with the row exponent of V

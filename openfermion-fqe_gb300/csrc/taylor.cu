@@ -116,8 +116,9 @@ size_t taylor_state_bytes() { return sizeof(TaylorState) + sizeof(double) * kTer
 
 // Records into the graph being captured on `cs`: psi -> work, the state's
 // reset, and the WHILE node of the series (its body captured on `bs`, a
-// stream that is not capturing, created by the caller before the capture).  work and next are the handle's two-vector buffer; `state` holds
-// a TaylorState followed by kTermBlocks partial sums.
+// stream that is not capturing, created by the caller before the capture).
+// work and next are the handle's two-vector buffer; `state` holds a
+// TaylorState followed by kTermBlocks partial sums.
 int taylor_record(fqegpu_ham h, double2* psi, double time, double accuracy, int expansion,
                   int precision, void* state, cudaStream_t cs, cudaStream_t bs) {
   const int64_t N = h->g->a.len * h->g->b.len;

@@ -316,6 +316,39 @@ class FqeData:
         assert h2e.shape == (norb * 2, norb * 2, norb * 2, norb * 2)
         return self._run_apply(ham_for(self._core, h1e, h2e, spin=True))
 
+    # -- orbital rotation and diagonal evolution ------------------------------
+    def apply_columns_recursive_inplace(self, mat1: numpy.ndarray,
+                                        mat2: numpy.ndarray) -> None:
+        """fqe_data.py:1510-1535: for every column icol, first of the alpha
+        strings with mat1 and then of the beta strings with mat2, the
+        column operator 1 + sum_i mat[i, icol] E_{i,icol}, applied in order
+        (fqegpu_transform; the work array is temporary device memory)."""
+        m1 = _host_c128(mat1)
+        m2 = _host_c128(mat2)
+        work = torch.empty_like(self.coeff)
+        _lib.call("fqegpu_transform", self._core.handle,
+                  m1.ctypes.data_as(ctypes.c_void_p),
+                  m2.ctypes.data_as(ctypes.c_void_p), _ptr(self.coeff),
+                  _ptr(work), _stream())
+
+    def evolve_diagonal(self, array: numpy.ndarray,
+                        inplace: bool = False) -> torch.Tensor:
+        """fqe_data.py:203-262: coeff[a, b] *= exp(sum_{i in a} array[i] +
+        sum_{j in b} array[beta_ptr + j]), array of size norb or 2 norb."""
+        norb = self.norb()
+        array = _host_c128(array).reshape(-1)
+        if array.size == 2 * norb:
+            da, db = array[:norb].copy(), array[norb:].copy()
+        elif array.size == norb:
+            da, db = array, array
+        else:
+            raise ValueError('Non-diagonal array passed into evolve_diagonal')
+        data = self.coeff if inplace else self.coeff.clone()
+        _lib.call("fqegpu_evolve_diagonal", self._core.handle,
+                  da.ctypes.data_as(ctypes.c_void_p),
+                  db.ctypes.data_as(ctypes.c_void_p), _ptr(data), _stream())
+        return data
+
     # -- diagonal Coulomb (fqe_data.py:263-402) ------------------------------
     def _diag_coulomb(self, diag, array, inplace: bool, mode: int):
         data = self.coeff if inplace else self.coeff.clone()
@@ -393,6 +426,21 @@ class FqeData:
                           device=self.coeff.device)
         _lib.call("fqegpu_diagonal", ham.handle, _ptr(out), _stream())
         return out
+
+    # pickling (Wavefunction.save / read): the sector and the coefficients as
+    # a host array; the string graph is rebuilt on the device when loaded
+    def __getstate__(self):
+        return {"nalpha": self.nalpha(), "nbeta": self.nbeta(),
+                "norb": self.norb(), "coeff": self.to_numpy()}
+
+    def __setstate__(self, state):
+        self._core = get_graph(state["nalpha"], state["nbeta"], state["norb"])
+        self._dtype = numpy.complex128
+        self._nele = state["nalpha"] + state["nbeta"]
+        self._m_s = state["nalpha"] - state["nbeta"]
+        self.coeff = torch.from_numpy(
+            numpy.ascontiguousarray(state["coeff"], dtype=numpy.complex128)).to(
+                settings.device())
 
     def __deepcopy__(self, memo):
         new = FqeData.__new__(FqeData)

@@ -18,8 +18,8 @@ What is modelled (csrc/ozaki.cu, k_oz_digits / k_oz_slice / k_oz_mma):
   are summed per K step of 16 pairs into four FP32 accumulators: levels 2,
   3, 4 alone (integer sums below 2^24 at one scale: exact) and levels 5..7
   together;
-* the four level sums are combined by an exact two-sum of levels 2 and 3,
-  the low part adding levels 4 and 5..7, and scaled by 2^(e_row + g0 + 1).
+* the four level sums are combined by a chain of exact two-sums (no level
+  is assumed to hold the leading bits) and scaled by 2^(e_row + g0 + 1).
 
 `contract` models the form the kernel had before: D's columns scaled by
 their exact exponents and rounded to 40-bit magnitudes (five slices, 19
@@ -94,6 +94,31 @@ def combine(acc, e_row, e_col):
     l2 = (l - (h2 - h)).astype(numpy.float32)
     scale = numpy.ldexp(1.0, e_row[:, None] + e_col[None, :])
     return (h2.astype(numpy.float64) + l2.astype(numpy.float64)) * scale
+
+
+def _two_sum(a, b):
+    s = (a + b).astype(numpy.float32)
+    bb = (s - a).astype(numpy.float32)
+    e = ((a - (s - bb)) + (b - bb)).astype(numpy.float32)
+    return s, e
+
+
+def combine_chain(acc, e_row, e_col):
+    """G from the level sums by a chain of exact two-sums in FP32:
+    (s, e) = two-sum(level 2, level 3), then s absorbs level 4 and levels
+    5..7 the same way, the rounding errors summed in e; (s + e) is
+    renormalised and scaled by 2^(e_row + e_col).  Unlike `combine` it does
+    not assume that levels 2 and 3 hold the leading bits, which fails when
+    D is scaled globally and a column's value starts in level 4 or later."""
+    a = [acc[i].astype(numpy.float32) for i in range(4)]
+    s, e = _two_sum(a[0], a[1])
+    for k in (2, 3):
+        s, e2 = _two_sum(s, a[k])
+        e = (e + e2).astype(numpy.float32)
+    h = (s + e).astype(numpy.float32)
+    l = (e - (h - s)).astype(numpy.float32)
+    scale = numpy.ldexp(1.0, e_row[:, None] + e_col[None, :])
+    return (h.astype(numpy.float64) + l.astype(numpy.float64)) * scale
 
 
 def psi_bound_exponents(psi):
@@ -194,7 +219,7 @@ def contract_psi_digits(V, psi, dvec, fp32=True):
     acc = digit_level_sums(vs, ds, fp32=fp32)
     M = ds[0].shape[1]
     e_col = numpy.full(M, g0 + 1)
-    G = combine(acc, e_row, e_col)
+    G = combine_chain(acc, e_row, e_col)
     n = M // 2
     return G[:, :n] + 1j * G[:, n:]
 

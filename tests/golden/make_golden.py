@@ -448,9 +448,54 @@ def chebyshev_fixture():
     save("chebyshev", **out)
 
 
+def quadratic_fixture():
+    """Wavefunction.time_evolve with a quadratic (one-body) restricted
+    Hamiltonian (wavefunction.py:1008-1032: diagonalising transformation,
+    transform, diagonal evolution, transform back), with e_0."""
+    out = {}
+    for norb, na, nb, seed in [(4, 2, 1, 0), (5, 2, 2, 1), (6, 3, 2, 2), (6, 3, 3, 3)]:
+        rng = numpy.random.default_rng(9100 + seed)
+        a = rng.normal(size=(norb, norb)) + 1j * rng.normal(size=(norb, norb))
+        h1 = 0.5 * (a + a.conj().T)
+        e0 = 0.3 - 0.1 * seed
+        lena, lenb = math.comb(norb, na), math.comb(norb, nb)
+        psi = synthetic.wavefunction_coeff(lena, lenb, rng)
+        w = fqe.Wavefunction([[na + nb, na - nb, norb]])
+        w.set_wfn(strategy="from_data", raw_data={(na + nb, na - nb): psi.copy()})
+        ham = fqe.get_restricted_hamiltonian((h1,), e_0=e0)
+        t = 0.7 + 0.1 * seed
+        res = w.time_evolve(t, ham)
+        tag = f"{norb}_{na}_{nb}_{seed}"
+        out[f"psi_{tag}"] = psi
+        out[f"h1_{tag}"] = h1
+        out[f"e0_{tag}"] = numpy.array(e0)
+        out[f"t_{tag}"] = numpy.array(t)
+        out[f"out_{tag}"] = res.get_coeff((na + nb, na - nb)).copy()
+    save("quadratic", **out)
+
+
+def saved_wfn_fixture():
+    """A file written by the reference's own Wavefunction.save
+    (wavefunction.py:747-765: a pickled list [symmetry map, conserved,
+    conserve_spin, conserve_number, norb, [key, FqeData], ...]) for three
+    sectors of norb 4, with the coefficients beside it in saved_wfn.npz."""
+    rng = numpy.random.default_rng(21)
+    wfn = fqe.Wavefunction([[4, 0, 4], [4, 2, 4], [4, -2, 4]])
+    out = {}
+    for key in wfn.sectors():
+        shape = wfn.get_coeff(key).shape
+        c = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+        wfn.set_wfn(strategy="from_data", raw_data={key: c})
+        out[f"coeff_{key[0]}_{key[1]}"] = c
+    wfn.save("ref_saved_wfn.pickle", path=HERE)
+    print("wrote", os.path.join(HERE, "ref_saved_wfn.pickle"))
+    save("saved_wfn", **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["graph", "apply", "dc", "taylor", "dvec",
                              "davidson", "rdm", "rdm12", "spin", "wfn_pickles",
-                             "transform", "chebyshev", "graph_pickles"]
+                             "transform", "chebyshev", "graph_pickles", "saved_wfn",
+                             "quadratic"]
     for name in which:
         globals()[name + "_fixture"]()

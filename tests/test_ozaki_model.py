@@ -142,6 +142,38 @@ def test_fewer_slices_would_break_the_bound(oracle):
     assert _rel(G5, V @ Dr) > 1e-9
 
 
+def test_digit_form_on_taylor_terms(oracle):
+    # the high-order terms of a Taylor series are more concentrated than a
+    # random psi; at one global scale their small columns start in level 4
+    # or later, where a combination that assumes levels 2-3 lead loses bits
+    # (1e-11 per apply, measured): the two-sum chain keeps them at ~5e-13
+    import ozaki_model as om
+    from fqe_gb300 import synthetic
+    norb, na, nb = 10, 5, 5
+    h1, h2, psi = synthetic.sector(norb, na, nb, 20, 4)
+    g = oracle.graph(norb, na, nb)
+    V = om.pair_matrix(h1, h2, na + nb, oracle.prep_spatial12).real.copy()
+    w = psi.copy()
+    for _ in range(18):
+        w = oracle.apply_spatial12(w, h1, h2, g)
+        w /= numpy.linalg.norm(w)
+    dv = _dvec(oracle, g, norb)
+    D = dv(w)
+    shape = (norb, norb, g.lena, g.lenb)
+    ref = oracle.make_coeff((V @ D).reshape(shape), g)
+    G = om.contract_psi_digits(V, w, dv)
+    assert _rel(oracle.make_coeff(G.reshape(shape), g), ref) < 2e-12
+    ds, g0 = om.digit_slices_of_dvec(w, dv)
+    vs = om.slices(V, om._exponents(V, 1)[:, None])
+    acc = om.digit_level_sums(vs, ds)
+    e_row = om._exponents(V, 1)
+    e_col = numpy.full(ds[0].shape[1], g0 + 1)
+    naive = om.combine(acc, e_row, e_col)
+    n = naive.shape[1] // 2
+    Gn = naive[:, :n] + 1j * naive[:, n:]
+    assert _rel(oracle.make_coeff(Gn.reshape(shape), g), ref) > 5e-12
+
+
 def test_digit_form_needs_level_7(oracle):
     # with psi's digits at one global exponent, dropping level 7 (15 instead
     # of 20 products) leaves psi effectively 40-bit at the global scale: too
