@@ -292,6 +292,16 @@ int fqegpu_evolve_diagonal(fqegpu_graph g, const double *h_diag_a,
  * stored; deterministic; synchronises on `stream`. */
 int fqegpu_rdm1(fqegpu_graph g, const double *d_bra, const double *d_ket,
                 double *h_rdm, void *stream);
+/* Two-particle RDM core: h_raw[kl][ij] = sum_I conj(D_bra[kl][I]) D_ket[ij][I]
+ * with D[ij][I] = <I|E_ij|.> (complex128 [norb^2][norb^2] on the host), the
+ * one GEMM of FqeData.rdm12's half-filling branch (fqe_data.py:1762-1781,
+ * whose dvecs come from calculate_dvec_spatial); the caller assembles
+ * rdm2 = -raw.reshape(n,n,n,n).transpose(1,2,0,3) plus rdm1 on the diagonal.
+ * D is formed on the fly from the pair tables and never stored (no dvec of
+ * norb^2 times the sector); FP64, deterministic; synchronises on `stream`.
+ * When d_bra == d_ket only the upper tiles are computed (Hermitian). */
+int fqegpu_rdm2_gram(fqegpu_graph g, const double *d_bra, const double *d_ket,
+                     double *h_raw, void *stream);
 
 /* ---- A10: Taylor propagator ------------------------------------------------
  * d_psi <- sum_k (-i t H)^k / k! d_psi until ||term|| < accuracy, at most

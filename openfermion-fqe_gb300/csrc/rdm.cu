@@ -1,4 +1,4 @@
-// One-particle reduced density matrix through the dvec gather.
+// One- and two-particle reduced density matrices through the dvec gather.
 //
 //   rdm1[i][j] = <bra| E_ij |ket> = sum_I conj(bra_I) D_ket[ij][I],
 //   D_ket[ij][I] = <I| E_ij |ket>, E_ij = sum_spin a+_i a_j
@@ -11,6 +11,7 @@
 // kRdmQ consecutive pairs; partial sums go to a [P][blocks] array reduced in
 // a fixed order, so the result is deterministic.
 #include <algorithm>
+#include <vector>
 
 #include "ham.cuh"
 
@@ -107,10 +108,168 @@ __global__ void k_rdm1_final(int nparts, const double2* __restrict__ partial,
   if (threadIdx.x == 0) out[blockIdx.x] = make_double2(sx[0], sy[0]);
 }
 
+// ---- two-particle RDM: the Gram matrix of the dvecs ------------------------
+//   raw[kl][ij] = sum_I conj(D_bra[kl][I]) D_ket[ij][I]
+// (the one complex GEMM of FqeData.rdm12's half-filling branch,
+// fqe_data.py:1762-1781, over the dvecs of calculate_dvec_spatial).  D is
+// never stored: each CTA owns a 32 x 32 tile of raw (bra pairs x ket pairs)
+// and a run of 32-determinant sub-blocks (one alpha row, 32 beta columns);
+// per sub-block it forms the tile's 32 bra and 32 ket D rows in shared memory
+// from psi through the pair tables, then accumulates in FP64.  Partial tiles
+// of the CTAs of one tile are summed in a fixed order (deterministic).
+
+constexpr int kGT = 32;    // tile edge (pairs)
+constexpr int kGSub = 32;  // determinants per sub-block
+
+__device__ __forceinline__ double2 dvec_value(int64_t p, int64_t lena, int64_t lenb, int64_t a,
+                                              int64_t b, const int32_t* __restrict__ tabA,
+                                              const int32_t* __restrict__ tabB,
+                                              const double2* __restrict__ psi) {
+  double vx = 0.0, vy = 0.0;
+  const int32_t ca = tabA[p * lena + a];
+  if (ca) {
+    const double2 x = psi[(int64_t)(abs(ca) - 1) * lenb + b];
+    const double s = ca > 0 ? 1.0 : -1.0;
+    vx = s * x.x;
+    vy = s * x.y;
+  }
+  const int32_t cb = tabB[p * lenb + b];
+  if (cb) {
+    const double2 x = psi[a * lenb + (abs(cb) - 1)];
+    const double s = cb > 0 ? 1.0 : -1.0;
+    vx += s * x.x;
+    vy += s * x.y;
+  }
+  return make_double2(vx, vy);
+}
+
+// grid.x: tiles (tr, tc) in row-major order over ntile x ntile (only
+// tr <= tc when `herm`), grid.y: chunks of sub-blocks.
+__global__ void __launch_bounds__(256) k_rdm2_gram(
+    int P, int ntile, int herm, int64_t lena, int64_t lenb, int64_t nsub_b,
+    const int32_t* __restrict__ tabA, const int32_t* __restrict__ tabB,
+    const double2* __restrict__ bra, const double2* __restrict__ ket,
+    const int32_t* __restrict__ tiles, double2* __restrict__ partial) {
+  __shared__ double2 sB[kGT][kGSub + 1];
+  __shared__ double2 sK[kGT][kGSub + 1];
+  const int tile = tiles[blockIdx.x];
+  const int tr = tile / ntile, tc = tile % ntile;
+  const int r = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 4;
+  double2 acc[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) acc[i] = make_double2(0.0, 0.0);
+  const int64_t nunits = lena * nsub_b;
+  const int64_t u0 = nunits * blockIdx.y / gridDim.y, u1 = nunits * (blockIdx.y + 1) / gridDim.y;
+  for (int64_t u = u0; u < u1; ++u) {
+    const int64_t a = u / nsub_b, b0 = (u - a * nsub_b) * kGSub;
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < 2 * kGT * kGSub; idx += blockDim.x) {
+      const int which = idx / (kGT * kGSub);
+      const int pp = (idx / kGSub) % kGT, d = idx % kGSub;
+      const int64_t b = b0 + d;
+      const int p = (which ? tc : tr) * kGT + pp;
+      double2 v = make_double2(0.0, 0.0);
+      if (p < P && b < lenb)
+        v = dvec_value(p, lena, lenb, a, b, tabA, tabB, which ? ket : bra);
+      if (which)
+        sK[pp][d] = v;
+      else
+        sB[pp][d] = v;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int d = 0; d < kGSub; ++d) {
+      const double2 x = sB[r][d];  // conj(x) * y
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const double2 y = sK[c0 + i][d];
+        acc[i].x += x.x * y.x + x.y * y.y;
+        acc[i].y += x.x * y.y - x.y * y.x;
+      }
+    }
+  }
+  double2* out = partial + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * kGT * kGT;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) out[r * kGT + c0 + i] = acc[i];
+  (void)herm;
+}
+
+// raw[P][P] from the partial tiles (fixed chunk order); the lower tiles of
+// a Hermitian Gram are the conjugate transposes of the upper ones.
+__global__ void k_rdm2_final(int P, int ntile, int herm, int ntiles, int nchunk,
+                             const int32_t* __restrict__ tiles,
+                             const double2* __restrict__ partial, double2* __restrict__ raw) {
+  const int t = blockIdx.x;
+  const int tile = tiles[t];
+  const int tr = tile / ntile, tc = tile % ntile;
+  for (int e = threadIdx.x; e < kGT * kGT; e += blockDim.x) {
+    double x = 0.0, y = 0.0;
+    for (int c = 0; c < nchunk; ++c) {
+      const double2 v = partial[((int64_t)c * ntiles + t) * kGT * kGT + e];
+      x += v.x;
+      y += v.y;
+    }
+    const int i = tr * kGT + e / kGT, j = tc * kGT + e % kGT;
+    if (i < P && j < P) {
+      raw[(int64_t)i * P + j] = make_double2(x, y);
+      if (herm && tr != tc) raw[(int64_t)j * P + i] = make_double2(x, -y);
+    }
+  }
+}
+
 }  // namespace
 }  // namespace fqegpu
 
 using namespace fqegpu;
+
+extern "C" int fqegpu_rdm2_gram(fqegpu_graph g, const double* d_bra, const double* d_ket,
+                                double* h_raw, void* stream) {
+  clear_error();
+  FQE_CHECK_ARG(g && d_bra && d_ket && h_raw, "NULL argument");
+  const int norb = g->norb;
+  const int P = norb * norb;
+  if (P == 0) return FQEGPU_OK;
+  const int64_t lena = g->a.len, lenb = g->b.len;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int ntile = (P + kGT - 1) / kGT;
+  const int herm = d_bra == d_ket ? 1 : 0;
+  std::vector<int32_t> tl;
+  for (int tr = 0; tr < ntile; ++tr)
+    for (int tc = herm ? tr : 0; tc < ntile; ++tc) tl.push_back(tr * ntile + tc);
+  const int ntiles = (int)tl.size();
+  const int64_t nsub_b = (lenb + kGSub - 1) / kGSub;
+  const int64_t nunits = lena * nsub_b;
+  // about four CTAs per SM in all
+  const int nchunk = (int)std::max<int64_t>(
+      1, std::min<int64_t>(nunits, (4 * kNumSMs + ntiles - 1) / ntiles));
+  const size_t pbytes = sizeof(double2) * (size_t)nchunk * ntiles * kGT * kGT;
+  const size_t rbytes = sizeof(double2) * (size_t)P * P;
+  char* scratch = nullptr;
+  FQE_CUDA(cudaMallocAsync(&scratch, pbytes + rbytes + sizeof(int32_t) * ntiles, st));
+  double2* partial = reinterpret_cast<double2*>(scratch);
+  double2* raw = reinterpret_cast<double2*>(scratch + pbytes);
+  int32_t* d_tiles = reinterpret_cast<int32_t*>(scratch + pbytes + rbytes);
+  cudaError_t e = cudaMemcpyAsync(d_tiles, tl.data(), sizeof(int32_t) * ntiles,
+                                  cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    k_rdm2_gram<<<dim3(ntiles, nchunk), 256, 0, st>>>(
+        P, ntile, herm, lena, lenb, nsub_b, g->a.tab_full, g->b.tab_full,
+        (const double2*)d_bra, (const double2*)d_ket, d_tiles, partial);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    k_rdm2_final<<<ntiles, 256, 0, st>>>(P, ntile, herm, ntiles, nchunk, d_tiles, partial, raw);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_raw, raw, rbytes, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFreeAsync(scratch, st);
+  if (e != cudaSuccess) {
+    set_error("rdm2: %s", cudaGetErrorString(e));
+    return FQEGPU_ERR_CUDA;
+  }
+  return FQEGPU_OK;
+}
 
 extern "C" int fqegpu_rdm1(fqegpu_graph g, const double* d_bra, const double* d_ket,
                            double* h_rdm, void* stream) {

@@ -67,6 +67,7 @@ _SIGNATURES = {
                       ctypes.POINTER(_I), _P],
     "fqegpu_diagonal": [_P, _P, _P],
     "fqegpu_rdm1": [_P, _P, _P, _P, _P],
+    "fqegpu_rdm2_gram": [_P, _P, _P, _P, _P],
     "fqegpu_transform": [_P, _P, _P, _P, _P, _P],
     "fqegpu_evolve_diagonal": [_P, _P, _P, _P, _P],
     "fqegpu_batch_create": [_I, _P, _P, _P, _D, _D, _D, _D, _I, _P,

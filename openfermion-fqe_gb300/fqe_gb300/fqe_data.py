@@ -100,18 +100,15 @@ def check_apply(ham: "_Ham") -> None:
     _lib.call("fqegpu_ham_check", ham.handle, _stream())
 
 
-def rdm2_from_dvecs(dket: torch.Tensor, dbra: torch.Tensor,
-                    rdm1: torch.Tensor) -> torch.Tensor:
-    """rdm2 of FqeData.rdm12 (fqe_data.py:1762-1781) from the dvecs
-    D[i, j, I] = <I|E_ij|.> of ket and bra ([norb, norb, lena, lenb]) and
-    rdm1[i][j] = <bra|E_ij|ket>: raw[k, l, i, j] = sum_I conj(D_bra[k, l, I])
-    D_ket[i, j, I] (one GEMM), rdm2 = -raw.permute(1, 2, 0, 3) and
+def rdm2_from_gram(raw: numpy.ndarray, rdm1: numpy.ndarray) -> numpy.ndarray:
+    """rdm2 of FqeData.rdm12 (fqe_data.py:1762-1781) from the Gram matrix
+    raw[kl][ij] = sum_I conj(D_bra[kl, I]) D_ket[ij, I] of the dvecs and
+    rdm1[i][j] = <bra|E_ij|ket>: rdm2 = -raw.reshape(n,n,n,n) permuted to
+    (l, i, k, j) order, i.e. rdm2[a, b, c, d] = -raw[c, a, b, d], and
     rdm2[:, i, i, :] += rdm1."""
-    norb = dket.shape[0]
-    p = norb * norb
-    raw = torch.matmul(dbra.reshape(p, -1).conj(),
-                       dket.reshape(p, -1).transpose(0, 1))
-    r2 = (-raw.reshape(norb, norb, norb, norb).permute(1, 2, 0, 3)).contiguous()
+    norb = rdm1.shape[0]
+    r2 = -numpy.ascontiguousarray(
+        raw.reshape(norb, norb, norb, norb).transpose(1, 2, 0, 3))
     for i in range(norb):
         r2[:, i, i, :] += rdm1
     return r2
@@ -407,17 +404,20 @@ class FqeData:
         reference that honour the bra agree with it): (rdm1, rdm2) with
         rdm1[i][j] = <bra| E_ij |self> and
         rdm2[a][b][c][d] = <bra| sum_st a+_as a+_bt a_cs a_dt |self>.
-        The dvecs come from fqegpu_make_dvec; their Gram matrix
-        D_bra^H D_ket is one complex GEMM (cuBLAS, FP64)."""
+        The Gram matrix of the two dvecs comes from fqegpu_rdm2_gram, which
+        forms the dvecs on the fly (no norb^2-times-sector array)."""
         bra = self if bradata is None else bradata
         if (bra.nalpha(), bra.nbeta(), bra.norb()) != (
                 self.nalpha(), self.nbeta(), self.norb()):
             raise ValueError("rdm12: bra and ket sectors differ")
         r1 = self.rdm1(bradata)[0]
-        dket = self.calculate_dvec_spatial()
-        dbra = dket if bra is self else bra.calculate_dvec_spatial()
-        r2 = rdm2_from_dvecs(dket, dbra, torch.from_numpy(r1).to(dket.device))
-        return r1, r2.cpu().numpy()
+        norb = self.norb()
+        raw = numpy.zeros((norb * norb, norb * norb), dtype=numpy.complex128)
+        if raw.size:
+            _lib.call("fqegpu_rdm2_gram", self._core.handle, _ptr(bra.coeff),
+                      _ptr(self.coeff), raw.ctypes.data_as(ctypes.c_void_p),
+                      _stream())
+        return r1, rdm2_from_gram(raw, r1)
 
     def diagonal_energies(self, h1e, h2e) -> torch.Tensor:
         """<I|H|I> for every determinant (Slater-Condon, one pass)."""

@@ -93,21 +93,23 @@ def test_no_cpu_fallback_without_device():
 
 
 def test_rdm2_assembly_matches_reference_fixture(golden, oracle):
-    # FqeData.rdm12's host-side assembly (GEMM of the dvecs, permutation,
-    # rdm1 on the diagonal), run on CPU tensors with the oracle's dvecs
-    import torch
-    from fqe_gb300.fqe_data import rdm2_from_dvecs
+    # FqeData.rdm12's host-side assembly (permutation of the dvecs' Gram
+    # matrix, rdm1 on the diagonal), with the Gram matrix formed here from
+    # the oracle's dvecs; the device computes the same Gram matrix
+    # (fqegpu_rdm2_gram, tests/test_gpu_rdm.py)
+    from fqe_gb300.fqe_data import rdm2_from_gram
     gd = golden("rdm12")
     for key in [k for k in gd if k.startswith("rdm2_")]:
         tag = key[5:]
         norb, na, nb = map(int, tag.split("_"))
         g = oracle.graph(norb, na, nb)
         ket, bra = gd["ket_" + tag], gd["bra_" + tag]
-        dket = torch.from_numpy(oracle.make_dvec(ket, g))
-        dbra = torch.from_numpy(oracle.make_dvec(bra, g))
-        r1 = torch.from_numpy(oracle.rdm1(ket, g))
-        r2 = rdm2_from_dvecs(dket, dket, r1).numpy()
+        p = norb * norb
+        dket = oracle.make_dvec(ket, g).reshape(p, -1)
+        dbra = oracle.make_dvec(bra, g).reshape(p, -1)
+        r1 = oracle.rdm1(ket, g)
+        r2 = rdm2_from_gram(dket.conj() @ dket.T, r1)
         assert numpy.abs(r2 - gd["rdm2_" + tag]).max() < 1e-13
-        t1 = torch.from_numpy(oracle.rdm1(ket, g, bra))
-        t2 = rdm2_from_dvecs(dket, dbra, t1).numpy()
+        t1 = oracle.rdm1(ket, g, bra)
+        t2 = rdm2_from_gram(dbra.conj() @ dket.T, t1)
         assert numpy.abs(t2 - gd["trdm2_" + tag]).max() < 1e-13
