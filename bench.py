@@ -23,6 +23,10 @@ same line (default sector norb=12 (6a,6b); --davidson-norb, --no-davidson).
                                  evolve), one JSON object
   python bench.py --norb 16 --precision ozaki --no-davidson
                                  the 165.6 M-determinant sector
+  python bench.py --taylor16     20 Taylor steps dt=0.05 at norb 16 (8a,8b) on
+                                 the tensor cores, first step against FP64
+  python bench.py --no-cpu-baseline --davidson-norb 16 --davidson-scratch-gb 60
+                                 Davidson to 1e-6 at norb 16, learned vs plain
 """
 
 import argparse
@@ -439,7 +443,12 @@ def davidson_leg(norb, subspace=32, scratch_gb=None, max_iter=400,
     kw = dict(block=4, tol=1e-6, max_subspace=subspace, max_iter=max_iter,
               precision=precision, verbose=verbose,
               scratch_limit=None if scratch_gb is None else int(scratch_gb * 2**30))
-    dav.davidson(ham, na, nb, **dict(kw, max_iter=2))  # plans, tables, caches
+    # warm-up of both arms: plans, tables, caches, the inference kernel
+    dav.davidson(ham, na, nb, **dict(kw, max_iter=2))
+    pre = None
+    if os.path.exists(precond.DEFAULT_WEIGHTS):
+        pre = precond.LearnedPreconditioner.load()
+        dav.davidson(ham, na, nb, preconditioner=pre, **dict(kw, max_iter=2))
     torch.cuda.synchronize()
 
     def row(r, extra=None):
@@ -455,10 +464,11 @@ def davidson_leg(norb, subspace=32, scratch_gb=None, max_iter=400,
                        f"Cholesky vectors, seed {SEED}; block 4, subspace <= {subspace},"
                        f" residual 1e-6, {precision} applies",
            "plain": row(plain), "learned": None}
-    if os.path.exists(precond.DEFAULT_WEIGHTS):
-        pre = precond.LearnedPreconditioner.load()
+    if pre is not None:
         learned = dav.davidson(ham, na, nb, preconditioner=pre, **kw)
-        out["learned"] = row(learned, {"fallbacks": pre.fallbacks})
+        out["learned"] = row(learned, {
+            "rejected_learned_vectors": learned.learned_rejected,
+            "switched_to_plain_at_iteration": learned.fallback_iteration})
         out["energy_difference"] = float(learned.eigenvalues[0]
                                          - plain.eigenvalues[0])
         out["time_ratio_learned_over_plain"] = learned.seconds / plain.seconds
@@ -547,6 +557,66 @@ def configs_leg():
     return out
 
 
+def taylor_leg(norb=16, steps=20, dt=0.05, accuracy=1e-12, fp64_check=True):
+    """The norb-16 (8a,8b) configuration: `steps` Taylor steps of dt on the
+    tensor cores (Ozaki-split BF16), per step the wall time, the number of
+    terms, the norm and the energy <psi|H|psi>; the first step also on the
+    FP64 GPU path, with the relative difference and the fidelity
+    |<psi_oz|psi_fp64>|^2 of the two results."""
+    import torch
+    import fqe_gb300
+    from fqe_gb300 import settings, synthetic
+    na, nb = norb // 2, norb - norb // 2
+    nchol = synthetic.default_nchol(norb)
+    h1, h2, psi = synthetic.sector(norb, na, nb, nchol, SEED)
+    ham = fqe_gb300.RestrictedHamiltonian((h1, h2))
+    key = (na + nb, na - nb)
+    w0 = fqe_gb300.Wavefunction([[na + nb, na - nb, norb]])
+    w0.set_wfn(strategy="from_data", raw_data={key: psi})
+    del psi
+    old = settings.precision
+    out = {"workload": f"norb={norb} ({na}a,{nb}b), {nchol} Cholesky vectors, seed {SEED}; "
+                       f"{steps} Taylor steps dt={dt} to {accuracy}"}
+    try:
+        settings.precision = "ozaki"
+        w = w0
+        rows = []
+        for k in range(steps):
+            torch.cuda.synchronize()
+            t0 = time.time()
+            w = w.apply_generated_unitary(dt, "taylor", ham, accuracy=accuracy,
+                                          expansion=80)
+            torch.cuda.synchronize()
+            sec = time.time() - t0
+            if k == 0:
+                first = w.get_coeff(key).clone()
+            e = complex(w.expectationValue(ham))
+            rows.append({"step": k + 1, "seconds": sec, "terms": w._taylor_terms,
+                         "norm_minus_1": w.norm() - 1.0, "energy": e.real,
+                         "energy_imag": e.imag})
+        out["ozaki_steps"] = rows
+        out["norm_drift_max"] = max(abs(r["norm_minus_1"]) for r in rows)
+        out["energy_drift_max"] = max(abs(r["energy"] - rows[0]["energy"]) for r in rows)
+        if fp64_check:
+            settings.precision = "fp64"
+            torch.cuda.synchronize()
+            t0 = time.time()
+            w64 = w0.apply_generated_unitary(dt, "taylor", ham, accuracy=accuracy,
+                                             expansion=80)
+            torch.cuda.synchronize()
+            ref = w64.get_coeff(key)
+            out["fp64_first_step_seconds"] = time.time() - t0
+            out["first_step_rel_diff_vs_fp64"] = float(
+                torch.linalg.norm(first - ref) / torch.linalg.norm(ref))
+            ov = torch.vdot(first.reshape(-1), ref.reshape(-1))
+            out["first_step_infidelity_vs_fp64"] = float(
+                1.0 - abs(ov) ** 2 / (torch.linalg.norm(first) ** 2 *
+                                      torch.linalg.norm(ref) ** 2))
+    finally:
+        settings.precision = old
+    return out
+
+
 def _block_w(ham):
     import numpy
     from fqe_gb300 import _lib
@@ -577,6 +647,9 @@ def main():
     ap.add_argument("--davidson-scratch-gb", type=float, default=None,
                     help="device workspace of the Davidson applies (GB)")
     ap.add_argument("--davidson-max-iter", type=int, default=400)
+    ap.add_argument("--taylor16", action="store_true",
+                    help="only the norb-16 (8a,8b) 20-step Taylor evolution "
+                         "(tensor cores) with the first step against FP64")
     ap.add_argument("--configs", action="store_true",
                     help="only measure the other single-GPU configurations "
                          "(norb 8 apply/Taylor; norb 14 FP64 vs tensor-core "
@@ -590,12 +663,15 @@ def main():
                      args.nchol or synthetic.default_nchol(args.norb))
     if args.impl == "reference":
         return run_reference(args)
-    if args.configs:
+    if args.configs or args.taylor16:
         import torch
         import fqe_gb300
         torch.cuda.set_device(0)
         fqe_gb300.build()
-        print(json.dumps({"configs": configs_leg()}), flush=True)
+        if args.taylor16:
+            print(json.dumps({"taylor_norb16": taylor_leg()}), flush=True)
+        else:
+            print(json.dumps({"configs": configs_leg()}), flush=True)
         return 0
     return run_gpu(args)
 

@@ -72,6 +72,9 @@ class DavidsonResult:
     residual_history: List[List[float]] = field(default_factory=list)
     seconds: float = 0.0
     fallback_iteration: Optional[int] = None  # learned -> plain switch
+    # learned correction vectors that added nothing to the subspace and were
+    # replaced by the plain one (before the switch)
+    learned_rejected: int = 0
 
 
 def _vdot(x: torch.Tensor, y: torch.Tensor) -> complex:
@@ -227,6 +230,7 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
     T = numpy.zeros((0, 0), dtype=numpy.complex128)
     converged = False
     fallback_it = None
+    rejected = 0
     best_hist: List[float] = []
     theta = numpy.zeros(nroots)
     X: List[torch.Tensor] = []
@@ -283,6 +287,7 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
                 added += 1
             elif hasattr(prec, "plain"):
                 # the learned vector lies in the subspace: plain fallback
+                rejected += 1
                 if orthonormal_add(prec.plain(R[j], float(w[j]), op.diag,
                                               op.graph)):
                     added += 1
@@ -290,7 +295,7 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
             break
     op.check()
     torch.cuda.synchronize()
-    return DavidsonResult(fallback_iteration=fallback_it,
+    return DavidsonResult(fallback_iteration=fallback_it, learned_rejected=rejected,
                           eigenvalues=numpy.array(theta), vectors=X[:nroots],
                           iterations=it, applies=op.applies,
                           converged=converged, residual_history=history,

@@ -71,7 +71,6 @@ class LearnedPreconditioner:
         self.floor = floor
         self._stats_key = None
         self._stats = None
-        self.fallbacks = 0
         self.set_params(numpy.zeros(NPARAM, numpy.float32)
                         if params is None else params)
 
@@ -132,7 +131,7 @@ class LearnedPreconditioner:
         return t
 
     def plain(self, r, theta, diag, graph):
-        self.fallbacks += 1
+        """The plain diagonal preconditioner (the fallback)."""
         t = torch.empty_like(r)
         _lib.call("fqegpu_precondition", r.numel(), _ptr(r), _ptr(diag),
                   float(theta), float(self.floor), _ptr(t), _stream())
