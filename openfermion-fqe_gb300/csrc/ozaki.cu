@@ -36,24 +36,20 @@
 //   k_oz_digits  the six digit planes of psi: [N] 16-byte words (digits 1-4,
 //               each a bf16x2 of the real and imaginary digit) and [N] 8-byte
 //               words (digits 5-6).
-//   k_oz_slice  one CTA per tile of 32 determinants (one alpha row): gathers
-//               the sources' digits through the per-pair target tables, adds
-//               them with their signs (bf16x2), and writes the six D slices
-//               to HBM already in the tensor core's shared-memory image
-//               (canonical no-swizzle K-major, 16-column K chunks, the two
-//               tiles of a tile pair interleaved chunk by chunk).
-//   k_oz_mma    persistent, one CTA per SM: a loader lane streams the slice
-//               images with cp.async.bulk into a ring of 16 KB slots (four K
-//               chunks of a tile pair each); the MMA warp runs the issue
-//               loop and lane 0 issues 128 x NP x 16 tcgen05.mma (A = 64
-//               determinants x re/im of the streamed chunk, B = V slices
-//               resident in shared memory); sixteen epilogue warps combine
-//               the four accumulators (single-buffered, 4 x NP TMEM columns)
-//               into G, stored coalesced as FP32 pairs [P][lena][w].
+//   k_oz_fused  persistent, one CTA per SM: producer warps gather the
+//               sources' digits through the per-pair target tables, add them
+//               with their signs (bf16x2, exact) and write the six D slices
+//               of a K chunk of a tile pair (64 determinants) straight into a
+//               shared-memory ring in the tensor core's canonical K-major
+//               image; the MMA warp issues 128 x NP x 16 tcgen05.mma (A = the
+//               D chunk, B = V slices resident in shared memory); sixteen
+//               epilogue warps combine the four TMEM accumulators into G,
+//               stored coalesced as FP32 pairs [P][lena][w].  No D image
+//               passes through HBM.
 //   k_oz_scatter  sigma from G in FP32-pair arithmetic.
-// Every wait in k_oz_mma is bounded; on a timeout the kernel records an
-// error, lets the other roles leave, waits for its issued copies and frees
-// its TMEM.
+// Every wait in k_oz_fused is bounded; on a timeout the kernel records an
+// error, lets the other roles leave and frees its TMEM (its only
+// asynchronous operations are MMAs, which it waits for).
 #include <cuda_bf16.h>
 #include <math_constants.h>
 
@@ -78,12 +74,13 @@ constexpr int kSuperTiles = 32;  // tiles per column super-block (1024 columns)
 constexpr int kChunkK = 16;    // K columns per streamed slice chunk (one MMA k-step)
 constexpr int kChunkElems = kN * kChunkK;  // 1024 BF16 = 2 KB
 constexpr int kPairChunkElems = 2 * kChunkElems;  // a K chunk of both tiles of a pair: 4 KB
-constexpr int kGroupK = 4;     // chunks per ring slot: one bulk copy, one wait, one commit
-constexpr int kMaxRing = 64;   // chunk ring depth (bounded by shared memory)
+constexpr int kSlotBytes = kDSlices * kPairChunkElems * 2;  // one K chunk, six slices: 24 KB
+constexpr int kMaxRing = 16;   // ring depth (bounded by shared memory)
 constexpr int kEpiWarps = 16;  // four per TMEM lane quarter, 32 columns each
 constexpr int kMmaWarp = 16;
-constexpr int kLoadWarp = 17;
-constexpr int kThreads = 18 * 32;
+constexpr int kProdWarp0 = 17;  // producer warps 17 .. 20
+constexpr int kProdWarps = 4;   // 128 threads: (64 determinants) x (2 octets of a chunk)
+constexpr int kThreads = (kProdWarp0 + kProdWarps) * 32;
 constexpr int kAccs = 4;           // levels 2, 3, 4 and 5..7
 constexpr uint32_t kTmemCols = kAccs * kNM;  // 512: one accumulator set
 constexpr long long kWaitCycles = 4000000000ll;  // default wait limit: ~2 s at 2 GHz
@@ -104,7 +101,6 @@ struct OzakiPlan {
   float4* d_G = nullptr;               // [P][lena][wb]
   int32_t* d_tabTA = nullptr;          // [lena][KP] target tables, pair index fastest
   int32_t* d_tabTB = nullptr;          // [lenb][KP]
-  __nv_bfloat16* d_dslices = nullptr;  // [tiles of a block][6][64 * KP] smem images
   // beta-column blocks only: per block and target column, the pairs whose
   // beta source lies in the block, CSR: offsets [nblk][lenb + 1], entries
   // (pair, sign * (source - c0 + 1))
@@ -142,7 +138,6 @@ struct OzArgs {
   const int32_t* misc;
   const __nv_bfloat16* vslices;
   const int32_t* vexp;
-  __nv_bfloat16* dslices;  // [ntiles][6][64 * KP]
   float4* G;
   int32_t* err;
   long long wait_cycles;  // limit of every bounded wait
@@ -219,124 +214,41 @@ __device__ __forceinline__ uint32_t digit_word(const uint4& a, const uint2& b, i
   return k == 0 ? a.x : k == 1 ? a.y : k == 2 ? a.z : k == 3 ? a.w : k == 4 ? b.x : b.y;
 }
 
-// ---- slicing: D tiles in the tensor core's shared-memory image ------------
-// One CTA (8 H warps) per tile of 32 determinants.  Warp w owns determinants
-// 4 (w % 8) .. 4 (w % 8) + 3 (MMA rows 8 (w % 8) .. + 7) and octets
-// 8 (w / 8) .. 8 (w / 8) + 7 of the pair index; lane l the determinant
-// 4 (w % 8) + (l & 3) and the octet 8 (w / 8) + (l >> 2).  For each of the
-// octet's eight pairs the thread reads the digit planes of its (at most) two
-// sources, flips their signs and adds them (bf16x2, exact), then writes per
-// slice the 8 real and 8 imaginary values as one 32-byte store of the
-// canonical K-major image (rows 2d and 2d + 1 of a core matrix).
-template <int H>  // H groups of eight octets: KP <= 64 H
-__global__ void __launch_bounds__(256 * H, H == 2 ? 2 : 1) k_oz_slice(OzArgs A) {
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int grp = w & 7, half = w >> 3;
-  const int64_t t = blockIdx.x;
-  const int KP = A.KP, noct = KP / 8;
-  const int o = 8 * half + (lane >> 2);
-  if (o >= noct) return;
-  int64_t ia64, ib064;
-  tile_coords(A, t, ia64, ib064);
-  const uint32_t lenb32 = (uint32_t)A.lenb;
-  const uint32_t ia = (uint32_t)ia64;
-  const int d = 4 * grp + (lane & 3);
-  const uint32_t ib = (uint32_t)ib064 + d;
-  const bool valid = ib < lenb32;
-  // the octet's eight table entries per spin: two 16-byte loads each
-  int4 ta0 = make_int4(0, 0, 0, 0), ta1 = ta0, tb0 = ta0, tb1 = ta0;
-  if (valid) {
-    const int4* pa = reinterpret_cast<const int4*>(A.tabTA + (size_t)ia * KP + 8 * o);
-    const int4* pb = reinterpret_cast<const int4*>(A.tabTB + (size_t)ib * KP + 8 * o);
-    ta0 = __ldg(pa);
-    ta1 = __ldg(pa + 1);
-    tb0 = __ldg(pb);
-    tb1 = __ldg(pb + 1);
-  }
-  const int32_t cas[8] = {ta0.x, ta0.y, ta0.z, ta0.w, ta1.x, ta1.y, ta1.z, ta1.w};
-  const int32_t cbs[8] = {tb0.x, tb0.y, tb0.z, tb0.w, tb1.x, tb1.y, tb1.z, tb1.w};
-  // re[k][j / 2], im[k][j / 2]: slice k of pairs j (low half) and j + 1
-  uint32_t re[kDSlices][4], im[kDSlices][4];
-#pragma unroll
-  for (int jp = 0; jp < 4; ++jp) {
-    uint32_t sum[2][kDSlices];
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int j = 2 * jp + u;
-      const int32_t ca = cas[j], cb = cbs[j];
-      uint4 a4 = make_uint4(0u, 0u, 0u, 0u), b4 = a4;
-      uint2 a2 = make_uint2(0u, 0u), b2 = a2;
-      if (ca) {
-        const uint32_t idx = (uint32_t)(abs(ca) - 1) * lenb32 + ib;
-        a4 = __ldg(A.pdA + idx);
-        a2 = __ldg(A.pdB + idx);
-      }
-      if (cb) {
-        const uint32_t idx = ia * lenb32 + (uint32_t)(abs(cb) - 1);
-        b4 = __ldg(A.pdA + idx);
-        b2 = __ldg(A.pdB + idx);
-      }
-      // a negative table entry flips the sign of both halves
-      const uint32_t ma = ca < 0 ? 0x80008000u : 0u, mb = cb < 0 ? 0x80008000u : 0u;
-#pragma unroll
-      for (int k = 0; k < kDSlices; ++k) {
-        const uint32_t x = digit_word(a4, a2, k) ^ ma, y = digit_word(b4, b2, k) ^ mb;
-        const __nv_bfloat162 z = __hadd2(*reinterpret_cast<const __nv_bfloat162*>(&x),
-                                         *reinterpret_cast<const __nv_bfloat162*>(&y));
-        sum[u][k] = *reinterpret_cast<const uint32_t*>(&z);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < kDSlices; ++k) {
-      re[k][jp] = __byte_perm(sum[0][k], sum[1][k], 0x5410u);  // the two real halves
-      im[k][jp] = __byte_perm(sum[0][k], sum[1][k], 0x7632u);  // the two imaginary halves
-    }
-  }
-  // image of a tile pair: [slice][K chunk][tile of the pair][64 x 16 canonical
-  // K-major], so one K chunk of both tiles (4 KB) is the 128-row A operand
-  const size_t chunk = (size_t)(KP / kChunkK) * kPairChunkElems;  // one slice
-  __nv_bfloat16* out = A.dslices + (size_t)(t >> 1) * kDSlices * chunk;
-  const uint32_t coff = (uint32_t)(o >> 1) * kPairChunkElems + (uint32_t)(t & 1) * kChunkElems;
-#pragma unroll
-  for (int k = 0; k < kDSlices; ++k) {
-    // rows 2d (real part) and 2d + 1 (imaginary part) are the two adjacent
-    // 16-byte rows of one core matrix: one 32-byte store (2d is even, so the
-    // address is 32-byte aligned)
-    __nv_bfloat16* q = out + (size_t)k * chunk + coff + tc::kmajor_offset(2 * d, 8 * (o & 1), kChunkK);
-    asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(q), "r"(re[k][0]),
-                 "r"(re[k][1]), "r"(re[k][2]), "r"(re[k][3]), "r"(im[k][0]), "r"(im[k][1]),
-                 "r"(im[k][2]), "r"(im[k][3])
-                 : "memory");
-  }
-}
-
-// ---- contraction: bulk-copied slices, tcgen05 MMAs, TMEM epilogue -----------
+// ---- the fused contraction: gather + digit slices + tcgen05 MMAs + epilogue --
 // One MMA tile is a pair of slice tiles: 64 determinants = 128 real rows.  The
-// MMA is G^T = D^T V^T: A = a 128-row K chunk of D slice b (streamed), B = V
-// slice a (KP rows = pairs, resident), D in TMEM = 128 lanes (determinant,
-// real/imaginary) x KP columns (pairs) per level accumulator (4 x KP <= 512
-// columns, single-buffered).  An MMA costs about the same time at N = 64 and
-// N = 128 here, so covering 64 determinants per instruction halves the
-// contraction time per determinant; with lanes = determinants the epilogue's
-// G stores are coalesced (a warp writes 16 determinants x 16 B of one pair).
-// Persistent, one CTA per SM, 18 warps: warps 0-15 epilogue (warp w reads TMEM
-// lanes 32 (w % 4) .. + 31 = 16 determinants of one slice tile, columns = the
-// pairs of group w / 4), warp 16 TMEM allocation + MMA issue (lane 0), warp 17
-// lane 0 streams the slice images into a ring of shared-memory slots with
-// cp.async.bulk (one slot = up to four 16-column K chunks of a tile pair).
-__global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
+// MMA is G^T = D^T V^T: A = a 128-row K chunk (16 pairs) of D slice b, B = V
+// slice a (NP rows = output pairs, resident in shared memory), D in TMEM = 128
+// lanes (determinant, real/imaginary) x NP columns per level accumulator
+// (4 x NP <= 512 columns, single-buffered); with lanes = determinants the
+// epilogue's G stores are coalesced (a warp writes 16 determinants x 16 B of
+// one pair).
+// Persistent, one CTA per SM, 21 warps:
+//   warps 0-15  epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (16
+//               determinants of one slice tile), columns = the pairs of group
+//               w / 4; combines the four level sums, scales, stores G;
+//   warp 16     TMEM allocation and the MMA issue loop (lane 0 issues);
+//   warps 17-20 producers: one thread per (determinant of the tile pair,
+//               octet of the K chunk).  For each K chunk they read the target
+//               tables of their eight pairs, gather the digit words of each
+//               pair's (at most two) sources, add them with their signs
+//               (bf16x2, exact) and write all six slices of the chunk into a
+//               ring slot of shared memory in the canonical no-swizzle K-major
+//               image; then fence.proxy.async and one mbarrier arrive per warp.
+// No D image goes through HBM: per determinant the kernel reads psi's digit
+// words (from L2, the tile order keeps them resident) and writes G.
+// The MMA loop runs K chunk outer, D slice, V slice inner; a ring slot holds
+// one K chunk of a tile pair with its six slices (24 KB) and is released
+// when its MMAs complete.
+__global__ void __maxnreg__(96) k_oz_fused(OzArgs A) {  // 21 warps x 96 registers
   extern __shared__ __align__(1024) unsigned char smem[];
   const int KP = A.KP, R = A.ring;
   const int NP = A.NP;
   const uint32_t v_elems = (uint32_t)NP * KP;
-  const uint32_t slot_elems = (uint32_t)(kGroupK * kPairChunkElems);
-  const uint32_t pchunk_bytes = (uint32_t)kPairChunkElems * 2u;
-  const int nch = KP / kChunkK;                       // chunks per slice
-  const int ngr = (nch + kGroupK - 1) / kGroupK;      // ring slots per slice
+  const int nch = KP / kChunkK;  // K chunks per tile pair
   const int64_t npairs = (A.ntiles + 1) / 2;
   __nv_bfloat16* sV = reinterpret_cast<__nv_bfloat16*>(smem);
-  __nv_bfloat16* sD = sV + kSlices * v_elems;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sD + (size_t)R * slot_elems);
+  unsigned char* sD = reinterpret_cast<unsigned char*>(sV + kSlices * v_elems);
+  uint64_t* full = reinterpret_cast<uint64_t*>(sD + (size_t)R * kSlotBytes);
   uint64_t* empty = full + kMaxRing;
   uint64_t* accfull = empty + kMaxRing;
   uint64_t* accempty = accfull + 1;
@@ -355,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   }
   if (tid == 0) {
     for (int i = 0; i < R; ++i) {
-      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&full[i], kProdWarps);
       tc::mbar_init(&empty[i], 1);
     }
     tc::mbar_init(accfull, 1);
@@ -376,72 +288,117 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   const int64_t t_begin = npairs * blockIdx.x / gridDim.x;
   const int64_t t_end = npairs * (blockIdx.x + 1) / gridDim.x;
 
-  if (warp == kLoadWarp) {
-    if (lane == 0) {
-      // ring position and phase advance incrementally (no 64-bit division)
-      int slot = 0;
-      uint32_t ph = 0;
-      int64_t issued = 0;      // slots filled (or, once, deliberately skipped)
-      int skipped = -1;        // ring index of the skipped fill (test injection)
-      uint32_t skipped_ph = 0;
-      bool ok = true;
-      for (int64_t t = t_begin; t < t_end && ok; ++t) {
-        const __nv_bfloat16* src =
-            A.dslices + (size_t)t * kDSlices * nch * kPairChunkElems;
-        for (int b = 0; b < kDSlices && ok; ++b) {
-          for (int gi = 0; gi < ngr; ++gi) {
-            const int c0 = gi * kGroupK;
-            const uint32_t bytes = (uint32_t)min(kGroupK, nch - c0) * pchunk_bytes;
-            if (!oz_wait(&empty[slot], ph ^ 1u, abort_flag, A.wait_cycles)) {
-              oz_abort(abort_flag, A.err, 5);
-              ok = false;
-              break;
+  if (warp >= kProdWarp0) {
+    // producer thread: determinant d of the tile pair (consecutive lanes take
+    // consecutive beta columns), octet o of every K chunk
+    const int pt = tid - kProdWarp0 * 32;
+    const int d = pt & 63, o = pt >> 6;
+    const int tile = d >> 5, dl = d & 31;
+    const uint32_t lenb32 = (uint32_t)A.lenb;
+    // byte offset of this thread's two rows (real, imaginary) in a slice
+    // region of a slot: tile half, core-matrix row 2 dl, k group o
+    const uint32_t roff =
+        (uint32_t)tile * (uint32_t)kChunkElems * 2u +
+        tc::kmajor_offset(2 * dl, 8 * o, kChunkK) * 2u;
+    const uint32_t sD0 = tc::smem_u32(sD);
+    int slot = 0;
+    uint32_t ph = 0;
+    bool ok = true;
+    for (int64_t t = t_begin; t < t_end && ok; ++t) {
+      const int64_t ts = 2 * t + tile;
+      int64_t ia64 = 0, ib064 = 0;
+      const bool live_tile = ts < A.ntiles;
+      if (live_tile) tile_coords(A, ts, ia64, ib064);
+      const uint32_t ia = (uint32_t)ia64;
+      const uint32_t ib = (uint32_t)ib064 + dl;
+      const bool valid = live_tile && ib < lenb32;
+      const int4* pa = reinterpret_cast<const int4*>(A.tabTA + (size_t)ia * KP + 8 * o);
+      const int4* pb = reinterpret_cast<const int4*>(A.tabTB + (size_t)ib * KP + 8 * o);
+      for (int c = 0; c < nch; ++c) {
+        // this chunk's eight table entries per spin: two 16-byte loads each
+        int4 ta0 = make_int4(0, 0, 0, 0), ta1 = ta0, tb0 = ta0, tb1 = ta0;
+        if (valid) {
+          ta0 = __ldg(pa + 4 * c);
+          ta1 = __ldg(pa + 4 * c + 1);
+          tb0 = __ldg(pb + 4 * c);
+          tb1 = __ldg(pb + 4 * c + 1);
+        }
+        const int32_t cas[8] = {ta0.x, ta0.y, ta0.z, ta0.w, ta1.x, ta1.y, ta1.z, ta1.w};
+        const int32_t cbs[8] = {tb0.x, tb0.y, tb0.z, tb0.w, tb1.x, tb1.y, tb1.z, tb1.w};
+        uint32_t re[kDSlices][4], im[kDSlices][4];
+#pragma unroll
+        for (int jp = 0; jp < 4; ++jp) {
+          uint32_t sum[2][kDSlices];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const int32_t ca = cas[2 * jp + u], cb = cbs[2 * jp + u];
+            uint4 a4 = make_uint4(0u, 0u, 0u, 0u), b4 = a4;
+            uint2 a2 = make_uint2(0u, 0u), b2 = a2;
+            if (ca) {
+              const uint32_t idx = (uint32_t)(abs(ca) - 1) * lenb32 + ib;
+              a4 = __ldg(A.pdA + idx);
+              a2 = __ldg(A.pdB + idx);
             }
-            const bool skip = A.skip_slot >= 0 && blockIdx.x == 0 && t == t_begin &&
-                              issued == A.skip_slot;
-            if (skip) {
-              // test injection: neither arrive nor copy, so the consumer's
-              // bounded wait on this slot runs out
-              skipped = slot;
-              skipped_ph = ph;
-            } else {
-              tc::mbar_arrive_expect_tx(&full[slot], bytes);
-              tc::bulk_g2s(sD + (size_t)slot * slot_elems,
-                           src + ((size_t)b * nch + c0) * kPairChunkElems, bytes, &full[slot]);
+            if (cb) {
+              const uint32_t idx = ia * lenb32 + (uint32_t)(abs(cb) - 1);
+              b4 = __ldg(A.pdA + idx);
+              b2 = __ldg(A.pdB + idx);
             }
-            ++issued;
-            if (++slot == R) {
-              slot = 0;
-              ph ^= 1u;
+            const uint32_t ma = ca < 0 ? 0x80008000u : 0u, mb = cb < 0 ? 0x80008000u : 0u;
+#pragma unroll
+            for (int k = 0; k < kDSlices; ++k) {
+              const uint32_t x = digit_word(a4, a2, k) ^ ma, y = digit_word(b4, b2, k) ^ mb;
+              const __nv_bfloat162 z = __hadd2(*reinterpret_cast<const __nv_bfloat162*>(&x),
+                                               *reinterpret_cast<const __nv_bfloat162*>(&y));
+              sum[u][k] = *reinterpret_cast<const uint32_t*>(&z);
             }
           }
+#pragma unroll
+          for (int k = 0; k < kDSlices; ++k) {
+            re[k][jp] = __byte_perm(sum[0][k], sum[1][k], 0x5410u);
+            im[k][jp] = __byte_perm(sum[0][k], sum[1][k], 0x7632u);
+          }
         }
-      }
-      // Before the CTA may exit, every bulk copy issued into shared memory
-      // must have landed: wait for the last fill of each slot (on the normal
-      // path the MMA warp has already consumed them all).
-      const int64_t nlast = issued < R ? issued : R;
-      int s2 = slot;
-      uint32_t p2 = ph;
-      for (int64_t k = 0; k < nlast; ++k) {
-        if (--s2 < 0) {
-          s2 = R - 1;
-          p2 ^= 1u;
+        // the slot must have been released by the MMAs of its last use
+        if (!__all_sync(0xffffffffu, oz_wait(&empty[slot], ph ^ 1u, abort_flag, A.wait_cycles))) {
+          if (lane == 0) oz_abort(abort_flag, A.err, 5);
+          ok = false;
+          break;
         }
-        if (s2 == skipped && p2 == skipped_ph) continue;
-        if (!oz_wait_drain(&full[s2], p2, A.wait_cycles + kWaitCycles)) oz_abort(abort_flag, A.err, 7);
+        const uint32_t base = sD0 + (uint32_t)slot * (uint32_t)kSlotBytes + roff;
+#pragma unroll
+        for (int k = 0; k < kDSlices; ++k) {
+          // rows 2 dl (real) and 2 dl + 1 (imaginary): 32 contiguous bytes
+          const uint32_t q = base + (uint32_t)k * (uint32_t)kPairChunkElems * 2u;
+          asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(q), "r"(re[k][0]),
+                       "r"(re[k][1]), "r"(re[k][2]), "r"(re[k][3])
+                       : "memory");
+          asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(q + 16u), "r"(im[k][0]),
+                       "r"(im[k][1]), "r"(im[k][2]), "r"(im[k][3])
+                       : "memory");
+        }
+        // generic-proxy writes -> visible to the tensor core (async proxy)
+        tc::fence_proxy_async_smem();
+        __syncwarp();
+        const bool skip = A.skip_slot >= 0 && blockIdx.x == 0 && t == t_begin &&
+                          c == A.skip_slot;  // test injection: this chunk never arrives
+        if (lane == 0 && !skip) tc::mbar_arrive(&full[slot]);
+        if (++slot == R) {
+          slot = 0;
+          ph ^= 1u;
+        }
       }
     }
   } else if (warp == kMmaWarp) {
     // The whole warp runs the issue loop, so descriptors and counters stay
     // warp-uniform; lane 0 alone issues the MMAs and commits.  Levels,
-    // accumulators and accumulate flags are compile-time after unrolling b,
-    // c and a: the issue loop is the contraction's limit, not the tensor pipe.
+    // accumulators and accumulate flags are compile-time after unrolling b
+    // and a.
     const uint32_t elect = lane == 0 ? 1u : 0u;
     const uint32_t idesc = tc::make_idesc_bf16(kM, (uint32_t)NP);
     const uint32_t sbo = (uint32_t)KP * 16u;          // V: full-K rows
     const uint32_t sbo_c = (uint32_t)kChunkK * 16u;   // D chunk: 16-column rows
-    // B = V slice descriptors of k-step 0; k-step ks adds 256 bytes = 16 units
+    // B = V slice descriptors of k-step 0; k-step c adds 256 bytes = 16 units
     uint64_t vdesc0[kSlices];
 #pragma unroll
     for (int a = 0; a < kSlices; ++a)
@@ -463,49 +420,38 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
         break;
       }
       tc::fence_after_sync();
-      // chunk group (b, gi): up to four 16-column K chunks of D slice b; a
-      // slot is released as soon as its MMAs complete
+      for (int c = 0; c < nch; ++c) {
+        if (!__all_sync(0xffffffffu, oz_wait(&full[slot], ph, abort_flag, A.wait_cycles))) {
+          if (elect) oz_abort(abort_flag, A.err, 3);
+          ok = false;
+          break;
+        }
+        tc::fence_after_sync();
+        // slice b of the chunk: a 4 KB region of the slot (256 units)
+        const uint64_t dd = tc::make_sdesc(sD0 + (uint32_t)slot * (uint32_t)kSlotBytes, 128,
+                                           sbo_c);
+        const uint64_t kb = (uint64_t)(16 * c);
+        // the first MMA into each accumulator of the tile pair (first chunk,
+        // b = 1, a <= 4) overwrites it
+        const uint32_t first = c == 0 ? 1u : 0u;
 #pragma unroll
-      for (int b = 1; b <= kDSlices; ++b) {
-        for (int gi = 0; gi < ngr && ok; ++gi) {
-          const int c0 = gi * kGroupK;
-          const int nk = min(kGroupK, nch - c0);
-          if (!__all_sync(0xffffffffu, oz_wait(&full[slot], ph, abort_flag, A.wait_cycles))) {
-            if (elect) oz_abort(abort_flag, A.err, 3);
-            ok = false;
-            break;
-          }
-          tc::fence_after_sync();
-          const uint64_t dd = tc::make_sdesc(sD0 + (uint32_t)slot * slot_elems * 2u, 128, sbo_c);
-          // k-step outer, V slice inner: consecutive MMAs go to different
-          // accumulators
+        for (int b = 1; b <= kDSlices; ++b) {
+          const uint64_t da = dd + (uint64_t)(256 * (b - 1));
 #pragma unroll
-          for (int c = 0; c < kGroupK; ++c) {
-            if (c < nk) {
-              // A (D chunk) advances one 4 KB pair chunk = 256 units per
-              // k-step; B (V slice a) advances 256 bytes = 16 units
-              const uint64_t da = dd + (uint64_t)(256 * c);
-              const uint64_t kb = (uint64_t)(16 * (c0 + c));
-              // the first MMA into each accumulator of the tile pair
-              // (b = 1, first chunk, a <= 4) overwrites it
-              const uint32_t first = (gi == 0 && c == 0) ? 1u : 0u;
-#pragma unroll
-              for (int a = 1; a <= kSlices; ++a) {
-                if (a + b <= kMaxLevel) {
-                  const int lvl = a + b;
-                  const int ai = lvl <= 4 ? lvl - 2 : 3;
-                  const uint32_t accum = (b == 1 && a <= 4) ? (first ^ 1u) : 1u;
-                  tc::mma_bf16_if(accs[ai], da, vdesc0[a - 1] + kb, idesc, accum, elect);
-                }
-              }
+          for (int a = 1; a <= kSlices; ++a) {
+            if (a + b <= kMaxLevel) {
+              const int lvl = a + b;
+              const int ai = lvl <= 4 ? lvl - 2 : 3;
+              const uint32_t accum = (b == 1 && a <= 4) ? (first ^ 1u) : 1u;
+              tc::mma_bf16_if(accs[ai], da, vdesc0[a - 1] + kb, idesc, accum, elect);
             }
           }
-          if (elect) tc::mma_commit(&empty[slot]);
-          __syncwarp();
-          if (++slot == R) {
-            slot = 0;
-            ph ^= 1u;
-          }
+        }
+        if (elect) tc::mma_commit(&empty[slot]);
+        __syncwarp();
+        if (++slot == R) {
+          slot = 0;
+          ph ^= 1u;
         }
       }
       if (!ok) break;
@@ -519,7 +465,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
       if (!oz_wait_drain(done, 0, A.wait_cycles + kWaitCycles)) oz_abort(abort_flag, A.err, 6);
     }
     __syncwarp();
-  } else {
+  } else if (warp < kEpiWarps) {
     const int quarter = warp & 3, cg = warp >> 2;
     const int row = 32 * quarter + lane;      // TMEM lane = MMA row
     const int half = row >> 6;                // slice tile of the pair
@@ -609,6 +555,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(OzArgs A) {
   tc::fence_after_sync();
   if (warp == kMmaWarp) tc::tmem_dealloc(tmem, kTmemCols);
 }
+
 
 // ---- pre-pass: global exponent and the fixed-point copy of psi ------------
 __device__ __forceinline__ int exp_of(double x) {
@@ -843,17 +790,17 @@ __global__ void k_oz_transpose_tab(int P, int KP, int64_t len, const int32_t* __
 // Shape of the tensor-core form for P pairs: K = KP (pairs rounded up to 16),
 // output pairs in npass passes of NP rows (four level accumulators of NP TMEM
 // columns, NP <= 128; five NP x KP V slices in shared memory beside a ring of
-// at least two slots).  False when the sector does not fit (FP64 kernels).
+// at least two 24 KB ring slots).  False when the sector does not fit (FP64
+// kernels).
 static bool oz_shape(int P, int smax, int& KP, int& npass, int& NP, size_t& fixed) {
   KP = (P + 15) / 16 * 16;
-  if (KP > 192) return false;  // the slicer covers 24 octets of pairs
+  if (KP > 192) return false;  // five NP x KP V slices beside two slots
   npass = KP <= kM ? 1 : 2;
   NP = ((P + npass - 1) / npass + 15) / 16 * 16;
   if (NP > kM) return false;
   fixed = sizeof(__nv_bfloat16) * (size_t)kSlices * NP * KP +
           sizeof(uint64_t) * (2 * kMaxRing + 3) + 16 + sizeof(int) * kM;
-  const size_t slot = sizeof(__nv_bfloat16) * (size_t)kGroupK * kPairChunkElems;
-  return fixed + 2 * slot <= (size_t)smax;
+  return fixed + 2 * (size_t)kSlotBytes <= (size_t)smax;
 }
 
 static int plan_create(fqegpu_ham h) {
@@ -907,10 +854,9 @@ static int plan_create(fqegpu_ham h) {
   FQE_CUDA(cudaMemcpy(pl->d_vexp, vexp.data(), sizeof(int32_t) * vexp.size(),
                       cudaMemcpyHostToDevice));
   const int64_t lena = h->g->a.len, lenb = h->g->b.len, N = lena * lenb;
-  // beta-column blocks: slice images (24 KP bytes: six BF16 slices of the
-  // real and imaginary part) and G (16 P bytes) per determinant of a block
-  // within the handle's scratch limit
-  const int64_t per_col = (int64_t)(2 * 2 * kDSlices * KP + 16 * P) * lena;
+  // beta-column blocks: G (16 P bytes per determinant) of a block within the
+  // handle's scratch limit
+  const int64_t per_col = (int64_t)(16 * P) * lena;
   int64_t wb = h->scratch_limit / std::max<int64_t>(per_col, 1);
   if (wb >= lenb) {
     wb = lenb;  // one block: G is [P][lena][lenb]
@@ -973,19 +919,13 @@ static int plan_create(fqegpu_ham h) {
       FQE_CUDA(cudaMemcpy(pl->d_bent, ent.data(), sizeof(int2) * ent.size(),
                           cudaMemcpyHostToDevice));
   }
-  const int64_t ntiles = lena * ((wb + kDets - 1) / kDets);  // tiles of the widest block
-  const int64_t npairs = (ntiles + 1) / 2;
-  const size_t dsl = sizeof(__nv_bfloat16) * (size_t)npairs * 2 * kDSlices * kN * KP;
-  FQE_CUDA(dev_alloc(&pl->d_dslices, dsl));
-  FQE_CUDA(cudaMemset(pl->d_dslices, 0, dsl));  // an unpaired last tile reads zeros
   FQE_CUDA(cudaDeviceGetAttribute(&pl->nsm, cudaDevAttrMultiProcessorCount, dev));
-  // as many slice slots as shared memory holds after the V slices
-  const size_t slot = sizeof(__nv_bfloat16) * (size_t)kGroupK * kPairChunkElems;
-  pl->ring = (int)std::min<size_t>(kMaxRing, ((size_t)smax - fixed) / slot);
-  pl->smem = fixed + (size_t)pl->ring * slot;
+  // as many ring slots as shared memory holds after the V slices
+  pl->ring = (int)std::min<size_t>(kMaxRing, ((size_t)smax - fixed) / kSlotBytes);
+  pl->smem = fixed + (size_t)pl->ring * kSlotBytes;
   // the attribute belongs to the kernel, not to this plan: set the device
   // maximum so plans of different sectors (different ring sizes) can coexist
-  FQE_CUDA(cudaFuncSetAttribute(k_oz_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+  FQE_CUDA(cudaFuncSetAttribute(k_oz_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
   return FQEGPU_OK;
 }
 
@@ -1055,7 +995,6 @@ void ozaki_destroy(fqegpu_ham h) {
   cudaFree(pl->d_G);
   cudaFree(pl->d_tabTA);
   cudaFree(pl->d_tabTB);
-  cudaFree(pl->d_dslices);
   cudaFree(pl->d_boff);
   cudaFree(pl->d_bent);
   if (pl->h_err) cudaFreeHost(pl->h_err);
@@ -1108,7 +1047,6 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   A.G = pl->d_G;
   A.tabTA = pl->d_tabTA;
   A.tabTB = pl->d_tabTB;
-  A.dslices = pl->d_dslices;
   A.err = pl->d_misc + 1;
   A.wait_cycles = pl->wait_cycles;
   A.skip_slot = pl->skip_slot;
@@ -1120,19 +1058,15 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
     A.c0 = c0;
     A.nb = (int)((w + kDets - 1) / kDets);
     A.ntiles = lena * (int64_t)A.nb;
+    // stage 0 -> 1: the digit pre-pass (first block only)
     if (blk > 0) FQE_TRY(stage_mark(h, blk, 0, st));
-    if (A.KP <= 128)
-      k_oz_slice<2><<<(unsigned)A.ntiles, 512, 0, st>>>(A);
-    else
-      k_oz_slice<3><<<(unsigned)A.ntiles, 768, 0, st>>>(A);
-    FQE_CUDA(cudaGetLastError());
     FQE_TRY(stage_mark(h, blk, 1, st));
     const int grid = (int)std::min<int64_t>(pl->nsm, (A.ntiles + 1) / 2);
     for (int pass = 0; pass < pl->npass; ++pass) {
       A.p0 = pass * pl->NP;
       A.vslices = pl->d_vslices + (size_t)pass * kSlices * vel;
       A.vexp = pl->d_vexp + (size_t)pass * pl->NP;
-      k_oz_mma<<<grid, kThreads, pl->smem, st>>>(A);
+      k_oz_fused<<<grid, kThreads, pl->smem, st>>>(A);
       FQE_CUDA(cudaGetLastError());
     }
     FQE_TRY(stage_mark(h, blk, 2, st));
