@@ -23,6 +23,8 @@ same line (default sector norb=12 (6a,6b); --davidson-norb, --no-davidson).
                                  evolve), one JSON object
   python bench.py --norb 16 --precision ozaki --no-davidson
                                  the 165.6 M-determinant sector
+  python bench.py --batch        256 uneven sectors (norb 8-12): apply and Taylor
+                                 graphs, default vs autotuned launch shape
   python bench.py --taylor16     20 Taylor steps dt=0.05 at norb 16 (8a,8b) on
                                  the tensor cores, first step against FP64
   python bench.py --no-cpu-baseline --davidson-norb 16 --davidson-scratch-gb 60
@@ -617,6 +619,98 @@ def taylor_leg(norb=16, steps=20, dt=0.05, accuracy=1e-12, fp64_check=True):
     return out
 
 
+BATCH_SHAPES = {8: [(4, 4), (5, 3), (3, 5), (4, 3), (5, 4)],
+                10: [(5, 5), (6, 4), (4, 5), (5, 4)],
+                12: [(6, 6), (5, 6), (6, 5), (7, 5)]}
+
+
+def batch_sectors(n=256):
+    """The batched configuration: n wavefunctions over norb {8, 10, 12} with
+    uneven (nalpha, nbeta), each with its own seeded integrals (seed = index)
+    and random normalised psi."""
+    from fqe_gb300 import synthetic
+    out = []
+    for i in range(n):
+        norb = (8, 10, 12)[i % 3]
+        shapes = BATCH_SHAPES[norb]
+        na, nb = shapes[(i // 3) % len(shapes)]
+        h1, h2, psi = synthetic.sector(norb, na, nb, synthetic.default_nchol(norb), i)
+        out.append((norb, na, nb, h1, h2, psi))
+    return out
+
+
+def batch_leg(n=256, reps=5):
+    """Benchmark configuration 3 on the tensor-core precision: n uneven
+    sectors' applies in one CUDA graph (fqegpu_batch_*) and their Taylor
+    evolutions t = 0.1 to 1e-10 in one graph (fqegpu_batch_taylor_*), with the
+    default launch shape ("fixed") and with the autotuner's per-shape choice
+    ("autotuned"); CUDA events around the graph launches."""
+    import gc
+    import torch
+    import fqe_gb300
+    from fqe_gb300 import autotune, settings
+    from fqe_gb300.batch import BatchApply, BatchTaylor
+    secs = batch_sectors(n)
+    ndet = sum(p[5].size for p in secs)
+    out = {"workload": f"{n} sectors, norb {{8,10,12}} uneven (nalpha, nbeta), "
+                       f"{ndet} determinants in all; apply + Taylor t=0.1 to 1e-10",
+           "determinants": ndet}
+
+    def datas():
+        ds = []
+        for norb, na, nb, h1, h2, psi in secs:
+            d = fqe_gb300.FqeData(na, nb, norb)
+            d.set_wfn(strategy="from_data", raw_data=psi)
+            ds.append(d)
+        return ds
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    arrays = [(p[3], p[4]) for p in secs]
+    old = settings.precision
+    settings.precision = "ozaki"
+    try:
+        for tuned in (False, True):
+            tag = "autotuned" if tuned else "fixed"
+            autotune.clear()
+            ds = datas()
+            b = BatchApply(ds, arrays, precision="ozaki", autotune=tuned)
+            b.launch()
+            b.check()
+            ms = min(timed(lambda: (b.launch(), b.check())) for _ in range(reps))
+            choices = {}
+            if tuned:
+                for k, v in autotune.cached().items():
+                    choices[f"{k[0]}_{k[1]}_{k[2]}"] = (
+                        "fp64" if v["fp64"] else f"tensor/super{v['super_tiles']}")
+            out[f"apply_{tag}"] = {"ms": ms, "det_per_s": ndet / (ms / 1e3)}
+            if tuned:
+                out["autotuned_choices"] = choices
+            del b
+            gc.collect()
+            ds = datas()
+            bt = BatchTaylor(ds, arrays, 0.1, accuracy=1e-10, expansion=80,
+                             precision="ozaki", autotune=tuned)
+            ms_t = timed(lambda: (bt.launch(), bt.terms()))
+            terms = bt.terms()
+            out[f"taylor_{tag}"] = {"ms": ms_t, "terms_min": min(terms),
+                                    "terms_max": max(terms)}
+            del bt, ds
+            gc.collect()
+            torch.cuda.empty_cache()
+    finally:
+        settings.precision = old
+    return out
+
+
 def _block_w(ham):
     import numpy
     from fqe_gb300 import _lib
@@ -647,6 +741,9 @@ def main():
     ap.add_argument("--davidson-scratch-gb", type=float, default=None,
                     help="device workspace of the Davidson applies (GB)")
     ap.add_argument("--davidson-max-iter", type=int, default=400)
+    ap.add_argument("--batch", action="store_true",
+                    help="only the batched configuration: 256 uneven sectors, "
+                         "apply and Taylor graphs, fixed vs autotuned")
     ap.add_argument("--taylor16", action="store_true",
                     help="only the norb-16 (8a,8b) 20-step Taylor evolution "
                          "(tensor cores) with the first step against FP64")
@@ -663,12 +760,14 @@ def main():
                      args.nchol or synthetic.default_nchol(args.norb))
     if args.impl == "reference":
         return run_reference(args)
-    if args.configs or args.taylor16:
+    if args.configs or args.taylor16 or args.batch:
         import torch
         import fqe_gb300
         torch.cuda.set_device(0)
         fqe_gb300.build()
-        if args.taylor16:
+        if args.batch:
+            print(json.dumps({"batch": batch_leg()}), flush=True)
+        elif args.taylor16:
             print(json.dumps({"taylor_norb16": taylor_leg()}), flush=True)
         else:
             print(json.dumps({"configs": configs_leg()}), flush=True)

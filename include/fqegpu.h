@@ -125,6 +125,15 @@ int fqegpu_ham_info(fqegpu_ham h, int64_t *info4);
  * since the batch's graph holds the current workspace. */
 int fqegpu_ham_set_scratch_limit(fqegpu_ham h, int64_t bytes);
 
+/* Tuning of the tensor-core form of this operator (no counterpart in the
+ * reference): super_tiles = column tiles of 32 determinants per super-block
+ * of the tile order (alpha rows inside a super-block, so psi's rows of one
+ * super-block stay in L2; 0 = unchanged, default 32); use_fp64 != 0 makes
+ * FQEGPU_PREC_OZAKI applies of this handle run the FP64 kernels (never less
+ * accurate; cheaper for small sectors).  Chosen per sector shape by the
+ * autotuner of the Python package (fqe_gb300.autotune). */
+int fqegpu_ham_set_tuning(fqegpu_ham h, int super_tiles, int use_fp64);
+
 /* Per-stage device time of the last apply on this handle (milliseconds,
  * summed over beta-column blocks): [0] gather (K2), [1] pair contraction
  * (K3), [2] scatter (K4).  Timing is measured with CUDA events recorded on

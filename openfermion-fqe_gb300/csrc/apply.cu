@@ -287,7 +287,8 @@ int apply_prepare(fqegpu_ham h, int precision) {
   if (h->zero || h->onebody) return FQEGPU_OK;
   if (precision == FQEGPU_PREC_OZAKI) {
     const int s = ozaki_prepare(h);
-    if (s != FQEGPU_ERR_UNSUPPORTED) return s;
+    if (s != FQEGPU_ERR_UNSUPPORTED && s != FQEGPU_OK) return s;
+    if (s == FQEGPU_OK && !ozaki_runs_fp64(h)) return FQEGPU_OK;
   }
   return ensure_workspace(h);
 }
@@ -789,6 +790,15 @@ extern "C" int fqegpu_ham_check(fqegpu_ham h, void* stream) {
   FQE_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
   if (h->oz) return ozaki_check(h, (cudaStream_t)stream);
   return FQEGPU_OK;
+}
+
+extern "C" int fqegpu_ham_set_tuning(fqegpu_ham h, int super_tiles, int use_fp64) {
+  clear_error();
+  FQE_CHECK_ARG(h != nullptr, "NULL handle");
+  FQE_CHECK_ARG(super_tiles >= 0 && super_tiles <= 4096, "super_tiles out of range");
+  const int s = ozaki_set_tuning(h, super_tiles, use_fp64);
+  // an operator without a tensor-core form always runs the FP64 kernels
+  return s == FQEGPU_ERR_UNSUPPORTED ? FQEGPU_OK : s;
 }
 
 extern "C" int fqegpu_ham_test_injection(fqegpu_ham h, int64_t wait_cycles, int skip_slot) {

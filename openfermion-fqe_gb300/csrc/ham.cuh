@@ -124,6 +124,13 @@ int ozaki_prepare(fqegpu_ham h);
 // error word: FQEGPU_ERR_TIMEOUT when a bounded wait gave up since the last
 // check.
 int ozaki_check(fqegpu_ham h, cudaStream_t st);
+// Tuning of the tensor-core path: tiles per column super-block (> 0; else
+// unchanged) and whether the operator runs the FP64 kernels instead.
+int ozaki_set_tuning(fqegpu_ham h, int super_tiles, int use_fp64);
+// Whether the tuned tensor-core path runs the FP64 kernels; a key of the
+// current tuning (recorded graphs are re-recorded when it changes).
+bool ozaki_runs_fp64(fqegpu_ham h);
+int ozaki_tuning_key(fqegpu_ham h);
 // Test-only: wait limit of the tensor-core kernel (cycles; <= 0: default) and
 // a ring slot of CTA 0's first tile pair left unfilled (-1: none).
 int ozaki_set_test_injection(fqegpu_ham h, long long wait_cycles, int skip_slot);

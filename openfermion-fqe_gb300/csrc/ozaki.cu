@@ -70,7 +70,7 @@ constexpr int kM = 128;        // MMA M (pairs, padded)
 constexpr int kN = 64;         // real columns of one slice tile
 constexpr int kNM = 128;       // MMA N: two slice tiles
 constexpr int kDets = 32;      // determinants per slice tile
-constexpr int kSuperTiles = 32;  // tiles per column super-block (1024 columns)
+constexpr int kSuperTiles = 32;  // default tiles per column super-block (1024 columns)
 constexpr int kChunkK = 16;    // K columns per streamed slice chunk (one MMA k-step)
 constexpr int kChunkElems = kN * kChunkK;  // 1024 BF16 = 2 KB
 constexpr int kPairChunkElems = 2 * kChunkElems;  // a K chunk of both tiles of a pair: 4 KB
@@ -121,6 +121,11 @@ struct OzakiPlan {
   // tile pair unfilled, so the MMA warp's wait on it must run out
   long long wait_cycles = kWaitCycles;
   int skip_slot = -1;
+  // tuning (fqegpu_ham_set_tuning): tiles per column super-block, and
+  // whether this operator runs the FP64 kernels (chosen by an autotuner for
+  // small sectors, where the tensor-core form's fixed costs dominate)
+  int super = kSuperTiles;
+  bool use_fp64 = false;
 };
 
 struct OzArgs {
@@ -129,6 +134,7 @@ struct OzArgs {
   int64_t lena, lenb, ntiles;  // ntiles: tiles of this beta-column block
   int nb;            // tiles per alpha row in this block
   int64_t c0, gld;   // first column of the block; row length of G (block width)
+  int super;         // tiles per column super-block of the tile order
   const int32_t* tabA;
   const int32_t* tabB;
   const int32_t* tabTA;  // [lena][KP]: the 8 pairs of an octet are 32 contiguous bytes
@@ -145,17 +151,17 @@ struct OzArgs {
 };
 
 // Tile t -> (alpha row, first beta column).  Tiles are visited in column
-// super-blocks of kSuperTiles tiles (1024 determinants of a row), alpha rows
+// super-blocks of A.super tiles (1024 determinants of a row), alpha rows
 // within a super-block: the 16-byte psi segments the alpha-source gathers read
 // (one 1024-column slice of every row, 16 KB each) then stay L2-resident.
 __device__ __forceinline__ void tile_coords(const OzArgs& A, int64_t t, int64_t& ia,
                                             int64_t& ib0) {
-  const int64_t per_super = A.lena * kSuperTiles;
+  const int64_t per_super = A.lena * A.super;
   const int64_t sb = t / per_super;
   const int64_t r = t - sb * per_super;
-  const int64_t w = min((int64_t)kSuperTiles, (int64_t)A.nb - sb * kSuperTiles);
+  const int64_t w = min((int64_t)A.super, (int64_t)A.nb - sb * A.super);
   ia = r / w;
-  ib0 = A.c0 + (sb * kSuperTiles + (r - ia * w)) * kDets;
+  ib0 = A.c0 + (sb * A.super + (r - ia * w)) * kDets;
 }
 
 // Bounded wait that also gives up when another role has aborted.
@@ -976,6 +982,19 @@ int ozaki_prepare(fqegpu_ham h) {
   return FQEGPU_OK;
 }
 
+bool ozaki_runs_fp64(fqegpu_ham h) { return h->oz && h->oz->use_fp64; }
+
+int ozaki_tuning_key(fqegpu_ham h) {
+  return h->oz ? (h->oz->super << 1) | (h->oz->use_fp64 ? 1 : 0) : -1;
+}
+
+int ozaki_set_tuning(fqegpu_ham h, int super_tiles, int use_fp64) {
+  FQE_TRY(ozaki_prepare(h));
+  if (super_tiles > 0) h->oz->super = super_tiles;
+  h->oz->use_fp64 = use_fp64 != 0;
+  return FQEGPU_OK;
+}
+
 int ozaki_set_test_injection(fqegpu_ham h, long long wait_cycles, int skip_slot) {
   FQE_TRY(ozaki_prepare(h));
   h->oz->wait_cycles = wait_cycles > 0 ? wait_cycles : kWaitCycles;
@@ -1021,6 +1040,7 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
     if (s == FQEGPU_ERR_UNSUPPORTED) return apply_fp64(h, psi, sigma, alpha, beta, st);
     FQE_TRY(s);
   }
+  if (h->oz->use_fp64) return apply_fp64(h, psi, sigma, alpha, beta, st);
   OzakiPlan* pl = h->oz;
   if (!h->defer_check) FQE_TRY(ozaki_poll(pl, st));
   const int32_t* tabA = ham_tabA(h);
@@ -1050,6 +1070,7 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
   A.err = pl->d_misc + 1;
   A.wait_cycles = pl->wait_cycles;
   A.skip_slot = pl->skip_slot;
+  A.super = pl->super;
   const size_t vel = (size_t)pl->NP * pl->KP;
   const double2 al = zmul_host(alpha, h->phase);
   int blk = 0;

@@ -212,6 +212,7 @@ struct TaylorGraph {
   void* ws = nullptr;
   const void* plan = nullptr;
   int64_t block_w = 0;
+  int tuning = -1;
 };
 
 void taylor_destroy(fqegpu_ham h) {
@@ -264,7 +265,8 @@ extern "C" int fqegpu_taylor(fqegpu_ham h, double* d_psi, double time,
   const bool same = tg->exec && tg->psi == psi && tg->time == time &&
                     tg->accuracy == accuracy && tg->expansion == expansion &&
                     tg->precision == precision && tg->ws == h->d_ws &&
-                    tg->plan == (const void*)h->oz && tg->block_w == h->block_w;
+                    tg->plan == (const void*)h->oz && tg->block_w == h->block_w &&
+                    tg->tuning == ozaki_tuning_key(h);
   if (!same) {
     drop_graph(tg);
     cudaStream_t cs = nullptr, bs = nullptr;
@@ -308,6 +310,7 @@ extern "C" int fqegpu_taylor(fqegpu_ham h, double* d_psi, double time,
     tg->ws = h->d_ws;
     tg->plan = h->oz;
     tg->block_w = h->block_w;
+    tg->tuning = ozaki_tuning_key(h);
   }
   FQE_CUDA(cudaGraphLaunch(tg->exec, st));
   FQE_CUDA(cudaMemcpyAsync(tg->h_state, tg->d_state, sizeof(TaylorState),

@@ -51,6 +51,7 @@ _SIGNATURES = {
     "fqegpu_apply": [_P, _P, _P, _D, _D, _D, _D, _I, _P],
     "fqegpu_apply_host": [_P, _P, _P, _D, _D, _D, _D, _I],
     "fqegpu_ham_check": [_P, _P],
+    "fqegpu_ham_set_tuning": [_P, _I, _I],
     "fqegpu_ham_test_injection": [_P, _L, _I],
     "fqegpu_debug_fail_allocs": [_I],
     "fqegpu_apply_noalloc": [_I, _I, _I, _P, _P, _P, _P, _D, _D, _D, _D, _P],

@@ -25,7 +25,8 @@ class BatchApply:
     def __init__(self, datas: Sequence[FqeData], arrays: Sequence[tuple],
                  alpha: complex = 1.0, beta: complex = 0.0,
                  precision: Optional[str] = None,
-                 scratch_limit: Optional[int] = None):
+                 scratch_limit: Optional[int] = None,
+                 autotune: bool = False):
         if len(datas) != len(arrays) or not datas:
             raise ValueError("one operator tuple per sector is required")
         self.datas = list(datas)
@@ -38,6 +39,8 @@ class BatchApply:
                 _lib.call("fqegpu_ham_set_scratch_limit", ham.handle,
                           int(scratch_limit))
             self.hams.append(ham)
+        if autotune:
+            _tune_all(self.datas, self.hams, precision)
         # the graph records these tensors' addresses: hold them for its life
         self.psis: List[torch.Tensor] = [d.coeff for d in self.datas]
         self.sigmas: List[torch.Tensor] = [torch.empty_like(d.coeff)
@@ -72,6 +75,16 @@ class BatchApply:
             self.handle = None
 
 
+def _tune_all(datas, hams, precision) -> None:
+    """The autotuner's choice (fqe_gb300.autotune) for every sector's handle,
+    one timing per sector shape."""
+    from . import autotune
+    prec = precision or ("ozaki" if settings.precision_code() == _lib.PREC_OZAKI
+                         else "fp64")
+    for d, h in zip(datas, hams):
+        autotune.apply_tuning(h, d, prec)
+
+
 class BatchTaylor:
     """Taylor evolution psi <- exp(-i t H) psi of many sectors in one CUDA
     graph (fqegpu_batch_taylor_create): every sector has its own operator
@@ -86,7 +99,7 @@ class BatchTaylor:
 
     def __init__(self, datas: Sequence[FqeData], arrays: Sequence[tuple],
                  time: float, accuracy: float = 1.0e-15, expansion: int = 30,
-                 precision: Optional[str] = None):
+                 precision: Optional[str] = None, autotune: bool = False):
         if len(datas) != len(arrays) or not datas:
             raise ValueError("one operator tuple per sector is required")
         self.datas = list(datas)
@@ -96,6 +109,8 @@ class BatchTaylor:
                 raise ValueError("operator tuples hold (h1,) or (h1, h2)")
             self.hams.append(_Ham(d._core, arr[0],
                                   arr[1] if len(arr) > 1 else None))
+        if autotune:
+            _tune_all(self.datas, self.hams, precision)
         # the graph evolves these tensors in place: hold them for its life
         self.psis: List[torch.Tensor] = [d.coeff for d in self.datas]
         code = (settings.precision_code() if precision is None else

@@ -76,3 +76,29 @@ def test_batch_follows_rebound_coefficients(gpu):
     del b
     gc.collect()
     _lib.call("fqegpu_ham_set_scratch_limit", ham0.handle, 1 << 30)  # released
+
+
+def test_autotuned_batch_matches_fixed(gpu, oracle):
+    """The autotuner (fqe_gb300.autotune) changes the launch shape, or the
+    kernels for small sectors, never the result beyond the tensor-core
+    tolerance; its choices are cached per sector shape."""
+    import torch
+    from fqe_gb300 import autotune, synthetic
+    from fqe_gb300.batch import BatchApply
+    autotune.clear()
+    datas, arrays = _setup(gpu)
+    arrays = [(a[0], synthetic.integrals(d.norb(), 2 * d.norb(), i)[1])
+              for i, (a, d) in enumerate(zip(arrays, datas))]
+    b0 = BatchApply(datas, arrays, precision="ozaki")
+    b1 = BatchApply(datas, arrays, precision="ozaki", autotune=True)
+    for b in (b0, b1):
+        b.launch()
+        b.check()
+    torch.cuda.synchronize()
+    assert autotune.cached()
+    for d, arr, s0, s1 in zip(datas, arrays, b0.sigmas, b1.sigmas):
+        g = oracle.graph(d.norb(), d.nalpha(), d.nbeta())
+        want = oracle.apply_spatial12(d.to_numpy(), arr[0], arr[1], g)
+        for s in (s0, s1):
+            got = s.cpu().numpy()
+            assert numpy.linalg.norm(got - want) / numpy.linalg.norm(want) < 1e-10
