@@ -330,8 +330,10 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_bwd(Feat F, int64_t n, const _
       for (int i = 0; i < kIn; ++i) fr[i] = 0.f;
     }
     __syncthreads();
-    // thread tid owns parameters p = tid + kTile * k
-#pragma unroll
+    // thread tid owns parameters p = tid + kTile * k (a rolled loop: the
+    // training kernels are off the apply path, and unrolling this loop made
+    // the file take minutes to compile)
+#pragma unroll 1
     for (int k = 0; k < kPerThread; ++k) {
       const int p = tid + kTile * k;
       if (p >= kParams) break;
