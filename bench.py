@@ -27,7 +27,7 @@ same line (default sector norb=12 (6a,6b); --davidson-norb, --no-davidson).
                                  graphs, default vs autotuned launch shape
   python bench.py --taylor16     20 Taylor steps dt=0.05 at norb 16 (8a,8b) on
                                  the tensor cores, first step against FP64
-  python bench.py --no-cpu-baseline --davidson-norb 16 --davidson-scratch-gb 60
+  python bench.py --no-cpu-baseline --davidson-norb 16 --davidson-scratch-gb 20
                                  Davidson to 1e-6 at norb 16, learned vs plain
 """
 
@@ -420,6 +420,14 @@ def run_gpu(args):
         "cpu_baseline": cpu,
     }
     if rank == 0 and world == 1 and not args.no_davidson:
+        # the headline sector's handles and buffers are released first: the
+        # Davidson subspace of a large sector needs the device memory
+        from fqe_gb300.fqe_data import clear_ham_cache
+        del ham, d, sigma, psi_pin, out_pin
+        clear_ham_cache()
+        import gc
+        gc.collect()
+        torch.cuda.empty_cache()
         line["davidson"] = davidson_leg(args.davidson_norb, args.davidson_subspace,
                                         args.davidson_scratch_gb,
                                         args.davidson_max_iter, prec)

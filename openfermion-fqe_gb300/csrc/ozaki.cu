@@ -76,11 +76,11 @@ constexpr int kChunkElems = kN * kChunkK;  // 1024 BF16 = 2 KB
 constexpr int kPairChunkElems = 2 * kChunkElems;  // a K chunk of both tiles of a pair: 4 KB
 constexpr int kSlotBytes = kDSlices * kPairChunkElems * 2;  // one K chunk, six slices: 24 KB
 constexpr int kMaxRing = 16;   // ring depth (bounded by shared memory)
-constexpr int kEpiWarps = 16;  // four per TMEM lane quarter, 32 columns each
-constexpr int kMmaWarp = 16;
-constexpr int kProdWarp0 = 17;  // producer warps 17 .. 20
-constexpr int kProdWarps = 4;   // 128 threads: (64 determinants) x (2 octets of a chunk)
-constexpr int kThreads = (kProdWarp0 + kProdWarps) * 32;
+constexpr int kEpiWarps = 8;   // two per TMEM lane quarter, NP / 2 columns each
+constexpr int kMmaWarp = 8;
+constexpr int kProdWarp0 = 9;   // producer warps 9 .. 16
+constexpr int kProdWarps = 8;   // 256 threads: (64 determinants) x (4 quarters of a chunk)
+constexpr int kThreads = (kProdWarp0 + kProdWarps) * 32;  // 17 warps: 20 for registers
 constexpr int kAccs = 4;           // levels 2, 3, 4 and 5..7
 constexpr uint32_t kTmemCols = kAccs * kNM;  // 512: one accumulator set
 constexpr long long kWaitCycles = 4000000000ll;  // default wait limit: ~2 s at 2 GHz
@@ -228,24 +228,27 @@ __device__ __forceinline__ uint32_t digit_word(const uint4& a, const uint2& b, i
 // (4 x NP <= 512 columns, single-buffered); with lanes = determinants the
 // epilogue's G stores are coalesced (a warp writes 16 determinants x 16 B of
 // one pair).
-// Persistent, one CTA per SM, 21 warps:
-//   warps 0-15  epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (16
-//               determinants of one slice tile), columns = the pairs of group
-//               w / 4; combines the four level sums, scales, stores G;
-//   warp 16     TMEM allocation and the MMA issue loop (lane 0 issues);
-//   warps 17-20 producers: one thread per (determinant of the tile pair,
-//               octet of the K chunk).  For each K chunk they read the target
-//               tables of their eight pairs, gather the digit words of each
-//               pair's (at most two) sources, add them with their signs
-//               (bf16x2, exact) and write all six slices of the chunk into a
-//               ring slot of shared memory in the canonical no-swizzle K-major
-//               image; then fence.proxy.async and one mbarrier arrive per warp.
+// Persistent, one CTA per SM, 17 warps (registers are granted to warps in
+// fours, so 17 warps at 96 registers fit where 21 did not):
+//   warps 0-7   epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (16
+//               determinants of one slice tile), columns = the pairs of half
+//               w / 4; combines the four level sums, scales and stores G four
+//               columns at a time, then releases the accumulators;
+//   warp 8      TMEM allocation and the MMA issue loop (lane 0 issues);
+//   warps 9-16  producers: one thread per (determinant of the tile pair,
+//               quarter of the K chunk = 4 pairs).  For each K chunk they
+//               read the target tables of their four pairs, gather the digit
+//               words of each pair's (at most two) sources, add them with
+//               their signs (bf16x2, exact) and write all six slices of the
+//               chunk into a ring slot of shared memory in the canonical
+//               no-swizzle K-major image; then fence.proxy.async and one
+//               mbarrier arrive per warp.
 // No D image goes through HBM: per determinant the kernel reads psi's digit
 // words (from L2, the tile order keeps them resident) and writes G.
 // The MMA loop runs K chunk outer, D slice, V slice inner; a ring slot holds
 // one K chunk of a tile pair with its six slices (24 KB) and is released
 // when its MMAs complete.
-__global__ void __maxnreg__(96) k_oz_fused(OzArgs A) {  // 21 warps x 96 registers
+__global__ void __launch_bounds__(kThreads, 1) k_oz_fused(OzArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int KP = A.KP, R = A.ring;
   const int NP = A.NP;
@@ -296,16 +299,17 @@ __global__ void __maxnreg__(96) k_oz_fused(OzArgs A) {  // 21 warps x 96 registe
 
   if (warp >= kProdWarp0) {
     // producer thread: determinant d of the tile pair (consecutive lanes take
-    // consecutive beta columns), octet o of every K chunk
+    // consecutive beta columns), quarter qq (pairs 4 qq .. 4 qq + 3) of every
+    // K chunk
     const int pt = tid - kProdWarp0 * 32;
-    const int d = pt & 63, o = pt >> 6;
+    const int d = pt & 63, qq = pt >> 6;
     const int tile = d >> 5, dl = d & 31;
     const uint32_t lenb32 = (uint32_t)A.lenb;
-    // byte offset of this thread's two rows (real, imaginary) in a slice
-    // region of a slot: tile half, core-matrix row 2 dl, k group o
+    // byte offset of this thread's two half rows (real, imaginary) in a
+    // slice region of a slot: tile half, core-matrix row 2 dl, k 4 qq
     const uint32_t roff =
         (uint32_t)tile * (uint32_t)kChunkElems * 2u +
-        tc::kmajor_offset(2 * dl, 8 * o, kChunkK) * 2u;
+        tc::kmajor_offset(2 * dl, 4 * qq, kChunkK) * 2u;
     const uint32_t sD0 = tc::smem_u32(sD);
     int slot = 0;
     uint32_t ph = 0;
@@ -318,22 +322,20 @@ __global__ void __maxnreg__(96) k_oz_fused(OzArgs A) {  // 21 warps x 96 registe
       const uint32_t ia = (uint32_t)ia64;
       const uint32_t ib = (uint32_t)ib064 + dl;
       const bool valid = live_tile && ib < lenb32;
-      const int4* pa = reinterpret_cast<const int4*>(A.tabTA + (size_t)ia * KP + 8 * o);
-      const int4* pb = reinterpret_cast<const int4*>(A.tabTB + (size_t)ib * KP + 8 * o);
+      const int4* pa = reinterpret_cast<const int4*>(A.tabTA + (size_t)ia * KP + 4 * qq);
+      const int4* pb = reinterpret_cast<const int4*>(A.tabTB + (size_t)ib * KP + 4 * qq);
       for (int c = 0; c < nch; ++c) {
-        // this chunk's eight table entries per spin: two 16-byte loads each
-        int4 ta0 = make_int4(0, 0, 0, 0), ta1 = ta0, tb0 = ta0, tb1 = ta0;
+        // this quarter's four table entries per spin: one 16-byte load each
+        int4 ta = make_int4(0, 0, 0, 0), tb = ta;
         if (valid) {
-          ta0 = __ldg(pa + 4 * c);
-          ta1 = __ldg(pa + 4 * c + 1);
-          tb0 = __ldg(pb + 4 * c);
-          tb1 = __ldg(pb + 4 * c + 1);
+          ta = __ldg(pa + 4 * c);
+          tb = __ldg(pb + 4 * c);
         }
-        const int32_t cas[8] = {ta0.x, ta0.y, ta0.z, ta0.w, ta1.x, ta1.y, ta1.z, ta1.w};
-        const int32_t cbs[8] = {tb0.x, tb0.y, tb0.z, tb0.w, tb1.x, tb1.y, tb1.z, tb1.w};
-        uint32_t re[kDSlices][4], im[kDSlices][4];
+        const int32_t cas[4] = {ta.x, ta.y, ta.z, ta.w};
+        const int32_t cbs[4] = {tb.x, tb.y, tb.z, tb.w};
+        uint32_t re[kDSlices][2], im[kDSlices][2];
 #pragma unroll
-        for (int jp = 0; jp < 4; ++jp) {
+        for (int jp = 0; jp < 2; ++jp) {
           uint32_t sum[2][kDSlices];
 #pragma unroll
           for (int u = 0; u < 2; ++u) {
@@ -374,13 +376,12 @@ __global__ void __maxnreg__(96) k_oz_fused(OzArgs A) {  // 21 warps x 96 registe
         const uint32_t base = sD0 + (uint32_t)slot * (uint32_t)kSlotBytes + roff;
 #pragma unroll
         for (int k = 0; k < kDSlices; ++k) {
-          // rows 2 dl (real) and 2 dl + 1 (imaginary): 32 contiguous bytes
+          // 8 bytes of row 2 dl (real) and 8 of row 2 dl + 1 (imaginary)
           const uint32_t q = base + (uint32_t)k * (uint32_t)kPairChunkElems * 2u;
-          asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(q), "r"(re[k][0]),
-                       "r"(re[k][1]), "r"(re[k][2]), "r"(re[k][3])
+          asm volatile("st.shared.v2.b32 [%0], {%1,%2};" ::"r"(q), "r"(re[k][0]), "r"(re[k][1])
                        : "memory");
-          asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(q + 16u), "r"(im[k][0]),
-                       "r"(im[k][1]), "r"(im[k][2]), "r"(im[k][3])
+          asm volatile("st.shared.v2.b32 [%0], {%1,%2};" ::"r"(q + 16u), "r"(im[k][0]),
+                       "r"(im[k][1])
                        : "memory");
         }
         // generic-proxy writes -> visible to the tensor core (async proxy)
@@ -477,10 +478,12 @@ __global__ void __maxnreg__(96) k_oz_fused(OzArgs A) {  // 21 warps x 96 registe
     const int half = row >> 6;                // slice tile of the pair
     const int det = (row & 63) >> 1;          // determinant in that tile
     const int part = row & 1;                 // 0 real, 1 imaginary
-    const int cw = NP / 4;                    // pairs per column group
+    const int cw = NP / 2;                    // pairs per column half (multiple of 8)
     const int pbeg = cg * cw;
+    const int nst = min(cw, A.P - A.p0 - pbeg);  // columns holding real pairs
     // D = 2^(g0 + 1) sum_b slice_b for every determinant (one global scale)
     const int colexp = A.misc[0] + 1;
+    const int64_t pstride = A.lena * A.gld * 2;  // float2 elements per pair row
     int64_t it = 0;
     for (int64_t t = t_begin; t < t_end; ++t, ++it) {
       const int64_t ts = 2 * t + half;
@@ -497,63 +500,50 @@ __global__ void __maxnreg__(96) k_oz_fused(OzArgs A) {  // 21 warps x 96 registe
       }
       tc::fence_after_sync();
       const uint32_t base = tmem + ((uint32_t)(32 * quarter) << 16);
-      // drain TMEM first: the four level sums of every column of this warp's
-      // group, combined into an FP32 pair (exact two-sum of levels 2 and 3,
-      // then levels 4 and 5..7), scaled, and held in registers; the
-      // accumulators are released before the G stores, so the next tile
-      // pair's MMAs run while this one's G goes out
-      float hreg[kM / 4], lreg[kM / 4];
+      // this lane's half of G[p][det]: (hi, lo) of the real or imaginary part
+      float2* gp = reinterpret_cast<float2*>(A.G + ia * A.gld + (ib - A.c0)) + part +
+                   (int64_t)(A.p0 + pbeg) * pstride;
+      // four columns at a time: the four level sums, combined into an FP32
+      // pair by a chain of exact two-sums (with one global scale a column's
+      // leading bits may sit in level 4 or later, so no level is assumed to
+      // dominate; the rounding errors are summed in l), scaled and stored
+      for (int c0 = 0; c0 < cw; c0 += 4) {
+        const int pc = pbeg + c0;
+        uint32_t ra[4], rb[4], rc[4], rd[4];
+        tc::tmem_ld4_nowait(base + (uint32_t)pc, ra);
+        tc::tmem_ld4_nowait(base + (uint32_t)(NP + pc), rb);
+        tc::tmem_ld4_nowait(base + (uint32_t)(2 * NP + pc), rc);
+        tc::tmem_ld4_nowait(base + (uint32_t)(3 * NP + pc), rd);
+        tc::tmem_wait_ld();
 #pragma unroll
-      for (int c0 = 0; c0 < kM / 4; c0 += 4) {
-        if (c0 < cw) {
-          const int pc = pbeg + c0;
-          uint32_t ra[4], rb[4], rc[4], rd[4];
-          tc::tmem_ld4_nowait(base + (uint32_t)pc, ra);
-          tc::tmem_ld4_nowait(base + (uint32_t)(NP + pc), rb);
-          tc::tmem_ld4_nowait(base + (uint32_t)(2 * NP + pc), rc);
-          tc::tmem_ld4_nowait(base + (uint32_t)(3 * NP + pc), rd);
-          tc::tmem_wait_ld();
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            // a chain of exact two-sums: with one global scale a column's
-            // leading bits may sit in level 4 or later, so no level is
-            // assumed to dominate; the rounding errors are summed in l
-            float h, l;
-            two_sum(__uint_as_float(ra[k]), __uint_as_float(rb[k]), h, l);
-            float e2;
-            two_sum(h, __uint_as_float(rc[k]), h, e2);
-            l += e2;
-            two_sum(h, __uint_as_float(rd[k]), h, e2);
-            l += e2;
-            const float h2 = h + l;
-            const float l2 = l - (h2 - h);
-            // with the row exponent of V
-            const int sc = sVexp[pc + k] + colexp;
-            if (sc >= -126 && sc <= 127) {
-              const float f = pow2f(sc);
-              hreg[c0 + k] = h2 * f;
-              lreg[c0 + k] = l2 * f;
-            } else {
-              hreg[c0 + k] = scale2(h2, sc);
-              lreg[c0 + k] = scale2(l2, sc);
-            }
+        for (int k = 0; k < 4; ++k) {
+          float h, l;
+          two_sum(__uint_as_float(ra[k]), __uint_as_float(rb[k]), h, l);
+          float e2;
+          two_sum(h, __uint_as_float(rc[k]), h, e2);
+          l += e2;
+          two_sum(h, __uint_as_float(rd[k]), h, e2);
+          l += e2;
+          const float h2 = h + l;
+          const float l2 = l - (h2 - h);
+          // with the row exponent of V
+          const int sc = sVexp[pc + k] + colexp;
+          float hs, ls;
+          if (sc >= -126 && sc <= 127) {
+            const float f = pow2f(sc);
+            hs = h2 * f;
+            ls = l2 * f;
+          } else {
+            hs = scale2(h2, sc);
+            ls = scale2(l2, sc);
           }
+          if (live && c0 + k < nst) gp[(int64_t)(c0 + k) * pstride] = make_float2(hs, ls);
         }
       }
+      // every TMEM load of this warp has completed (wait::ld above): release
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(accempty);
-      if (!live) continue;
-      // this lane's half of G[p][det]: (hi, lo) of the real or imaginary part
-      const int64_t pstride = A.lena * A.gld * 2;  // float2 elements per pair row
-      float2* gp = reinterpret_cast<float2*>(A.G + ia * A.gld + (ib - A.c0)) + part +
-                   (int64_t)(A.p0 + pbeg) * pstride;
-      const int nst = min(cw, A.P - A.p0 - pbeg);  // columns holding real pairs
-#pragma unroll
-      for (int c = 0; c < kM / 4; ++c) {
-        if (c < nst) *gp = make_float2(hreg[c], lreg[c]);
-        gp += pstride;
-      }
     }
   }
   tc::fence_before_sync();

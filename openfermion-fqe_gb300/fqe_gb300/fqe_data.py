@@ -94,6 +94,12 @@ def ham_for(graph: FciGraph, h1, h2, spin: bool = False) -> _Ham:
     return ham
 
 
+def clear_ham_cache() -> None:
+    """Drops the cached Hamiltonian handles (their device workspaces are
+    freed once nothing else holds them)."""
+    _HAM_CACHE.clear()
+
+
 def check_apply(ham: "_Ham") -> None:
     """Waits for the current stream and raises TimeoutError if a tensor-core
     apply of `ham` gave up a bounded device wait since the last check."""
