@@ -59,6 +59,9 @@ def set_workload(norb, nalpha, nbeta, nchol):
 UNIT = "det/s"
 # the tensor-core contraction: BF16 slices of D (psi's digits) and products
 OZ_DSLICES, OZ_PRODUCTS = 6, 20
+# DRAM bytes of one k_oz_fused launch over its algorithmic bytes, from the
+# norb-12 ncu capture (profiles/k_oz_fused_norb12.md)
+FUSED_TRAFFIC_RATIO = 1.03
 
 
 def peaks():
@@ -323,13 +326,12 @@ def run_gpu(args):
     # P x P x N; gather writes and scatter reads D/G at 16 B per element)
     KP = (P + 15) // 16 * 16
     if prec == "ozaki":
-        # slicing kernel writes 6 BF16 slices of 64 x KP per 32-det tile
-        # (reading psi's 24-byte digit words, once per determinant at least);
-        # contraction: 20 useful BF16 products of P x P x (2 real columns)
-        ntiles = d.lena() * ((d.lenb() + 31) // 32)
-        slice_bytes = ntiles * OZ_DSLICES * 64 * KP * 2.0
+        # stage "gather": the digit pre-pass (k_oz_rowexp reads psi, k_oz_digits
+        # reads psi and writes the 24-byte digit words); stage "contraction":
+        # k_oz_fused (gathers the digits from L2, forms D in shared memory,
+        # 20 useful BF16 products of P x P x (2 real columns), writes G)
         contract_flops = OZ_PRODUCTS * 2.0 * P * P * 2.0 * n
-        gather_bytes = 16.0 * n + slice_bytes + 24.0 * n
+        gather_bytes = 16.0 * n + 16.0 * n + 24.0 * n
     else:
         contract_flops = 2.0 * 2.0 * P * P * n
         gather_bytes = 16.0 * n + 16.0 * P * n
@@ -353,19 +355,11 @@ def run_gpu(args):
     dk = stages[names[dom]]
     traffic = None
     if prec == "ozaki" and names[dom] == "contraction":
-        # k_oz_mma DRAM bytes per launch: a full ncu capture of the same kernel
-        # at norb 12 measured 0.98 x its algorithmic bytes (slice images read
+        # k_oz_fused DRAM bytes per launch: the full ncu capture of the same
+        # kernel at norb 12 (profiles/k_oz_fused_norb12.md) measured
+        # FUSED_TRAFFIC_RATIO x its algorithmic bytes (psi's digit words read
         # once, G written once); scaled to this workload's algorithmic bytes
-        ntiles = d.lena() * ((d.lenb() + 31) // 32)
-        images = 2 * ((ntiles + 1) // 2) * OZ_DSLICES * 64 * KP * 2.0
-        traffic = 0.98 * (images + 16.0 * P * n)
-    elif prec == "ozaki" and names[dom] == "gather":
-        # k_oz_slice DRAM bytes per launch: the norb-12 capture measured 1.386 GB
-        # (0.073 read + 1.313 written) for 1.372 GB of slice images = 1.01 x
-        # the images it writes; scaled to this workload's images (the small
-        # exponent and fixed-point pre-passes of the stage are not included)
-        ntiles = d.lena() * ((d.lenb() + 31) // 32)
-        traffic = 1.01 * 2 * ((ntiles + 1) // 2) * OZ_DSLICES * 64 * KP * 2.0
+        traffic = FUSED_TRAFFIC_RATIO * (24.0 * n + 16.0 * P * n)
     roofline = {"kernel": names[dom], "bound": dk["bound"],
                 "achieved": dk["achieved"], "peak": dk["peak"],
                 "unit": dk["unit"],
@@ -391,7 +385,7 @@ def run_gpu(args):
                          f"(reference C algorithm restated, OpenMP) took {t_cpu:.2f} s"}
 
     if prec == "ozaki":
-        launches_per_apply = 6  # rowexp, globalexp, fixed, slice, mma, scatter
+        launches_per_apply = 5  # rowexp, globalexp, digits, fused, scatter
     else:
         launches_per_apply = 3 * math.ceil(d.lenb() / max(1, _block_w(ham)))
     line = {
