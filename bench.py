@@ -743,6 +743,8 @@ def main():
     ap.add_argument("--davidson-scratch-gb", type=float, default=None,
                     help="device workspace of the Davidson applies (GB)")
     ap.add_argument("--davidson-max-iter", type=int, default=400)
+    ap.add_argument("--no-fp64-check", action="store_true",
+                    help="with --taylor16: skip the first step's FP64 comparison")
     ap.add_argument("--batch", action="store_true",
                     help="only the batched configuration: 256 uneven sectors, "
                          "apply and Taylor graphs, fixed vs autotuned")
@@ -770,7 +772,8 @@ def main():
         if args.batch:
             print(json.dumps({"batch": batch_leg()}), flush=True)
         elif args.taylor16:
-            print(json.dumps({"taylor_norb16": taylor_leg()}), flush=True)
+            print(json.dumps({"taylor_norb16": taylor_leg(
+                fp64_check=not args.no_fp64_check)}), flush=True)
         else:
             print(json.dumps({"configs": configs_leg()}), flush=True)
         return 0
