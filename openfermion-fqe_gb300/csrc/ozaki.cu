@@ -24,9 +24,10 @@
 // share one accumulator whose FP32 rounding sits ~2^-48 below level 2.
 // Levels >= 8 are dropped: 20 BF16 products per tile (a <= 5, b <= 6).  The
 // four accumulators are combined by a chain of exact two-sums into an FP32
-// pair (hi + lo, ~48 bits; no level is assumed to hold the leading bits,
-// since at one global scale a small column starts in level 4 or later) and
-// scaled by 2^{eV(p) + g0 + 1}.  Modelled error on sigma (numpy model,
+// pair (h, l) (h the rounded sum, l the summed rounding errors: ~48 bits; no
+// level is assumed to hold the leading bits, since at one global scale a
+// small column starts in level 4 or later), left unnormalised for the
+// scatter's FP32-pair sum, and scaled by 2^{eV(p) + g0 + 1}.  Modelled error on sigma (numpy model,
 // tests/test_ozaki_model.py): ~1e-12 for a spread-out psi, 2-3e-12 for one
 // concentrated on a few determinants, ~5e-13 for the high-order terms of a
 // Taylor series, against 1.7-4.6e-12 for exact per-determinant exponents.
@@ -36,16 +37,19 @@
 //   k_oz_digits  the six digit planes of psi: [N] 16-byte words (digits 1-4,
 //               each a bf16x2 of the real and imaginary digit) and [N] 8-byte
 //               words (digits 5-6).
-//   k_oz_fused  persistent, one CTA per SM: producer warps gather the
-//               sources' digits through the per-pair target tables, add them
-//               with their signs (bf16x2, exact) and write the six D slices
-//               of a K chunk of a tile pair (64 determinants) straight into a
-//               shared-memory ring in the tensor core's canonical K-major
-//               image; the MMA warp issues 128 x NP x 16 tcgen05.mma (A = the
-//               D chunk, B = V slices resident in shared memory); sixteen
-//               epilogue warps combine the four TMEM accumulators into G,
-//               stored coalesced as FP32 pairs [P][lena][w].  No D image
-//               passes through HBM.
+//   k_oz_fused  persistent, one CTA per SM: eight producer warps gather the
+//               sources' digits through the per-pair target tables (table
+//               entries loaded one K chunk ahead), add them with their signs
+//               (bf16x2, exact) and write the six D slices of a K chunk of a
+//               tile pair (64 determinants) straight into a shared-memory
+//               ring in the tensor core's canonical K-major image, one
+//               bank-conflict-free 16-byte row per lane and slice; the MMA
+//               warp issues 128 x NP x 16 tcgen05.mma (A = the D chunk, B = V
+//               slices resident in shared memory); eight epilogue warps drain
+//               the four TMEM accumulators (loads of the next four columns in
+//               flight while the current four are combined), release them
+//               before their last stores, and store G coalesced as FP32 pairs
+//               [P][lena][w].  No D image passes through HBM.
 //   k_oz_scatter  sigma from G in FP32-pair arithmetic.
 // Every wait in k_oz_fused is bounded; on a timeout the kernel records an
 // error, lets the other roles leave and frees its TMEM (its only
@@ -80,7 +84,8 @@ constexpr int kEpiWarps = 8;   // two per TMEM lane quarter, NP / 2 columns each
 constexpr int kMmaWarp = 8;
 constexpr int kProdWarp0 = 9;   // producer warps 9 .. 16
 constexpr int kProdWarps = 8;   // 256 threads: (64 determinants) x (4 quarters of a chunk)
-constexpr int kThreads = (kProdWarp0 + kProdWarps) * 32;  // 17 warps: 20 for registers
+constexpr int kThreads = (kProdWarp0 + kProdWarps) * 32;  // 17 warps
+constexpr int kRegWarps = 20;  // register budget of the launch bounds
 constexpr int kAccs = 4;           // levels 2, 3, 4 and 5..7
 constexpr uint32_t kTmemCols = kAccs * kNM;  // 512: one accumulator set
 constexpr long long kWaitCycles = 4000000000ll;  // default wait limit: ~2 s at 2 GHz
@@ -200,6 +205,10 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
+// Accumulator of the product of V slice a and D digit b: levels 2, 3, 4 and
+// 5..7.
+__host__ __device__ constexpr int acc_of(int a, int b) { return a + b <= 4 ? a + b - 2 : 3; }
+
 // 2^e as a float for -126 <= e <= 127.
 __device__ __forceinline__ float pow2f(int e) {
   return __int_as_float((e + 127) << 23);
@@ -248,7 +257,10 @@ __device__ __forceinline__ uint32_t digit_word(const uint4& a, const uint2& b, i
 // The MMA loop runs K chunk outer, D slice, V slice inner; a ring slot holds
 // one K chunk of a tile pair with its six slices (24 KB) and is released
 // when its MMAs complete.
-__global__ void __launch_bounds__(kThreads, 1) k_oz_fused(OzArgs A) {
+// Register cap: the 17 warps are spread over the four SM sub-partitions (16K
+// registers each), five on one of them, so a thread may hold at most 96
+// registers; bounds of 20 warps make the compiler keep to that.
+__global__ void __launch_bounds__(kRegWarps * 32, 1) k_oz_fused(OzArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
   const int KP = A.KP, R = A.ring;
   const int NP = A.NP;
@@ -265,6 +277,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_fused(OzArgs A) {
   uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
   int* sVexp = reinterpret_cast<int*>(tslot + 2);  // [kM] row exponents of V
+  // [kM] 2^(eV(p) + g0 + 1) per output pair, 0 where outside FP32's range
+  float* sScale = reinterpret_cast<float*>(sVexp + kM);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   {
@@ -272,7 +286,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_fused(OzArgs A) {
     int4* dst = reinterpret_cast<int4*>(sV);
     const int n16 = (int)(kSlices * v_elems * 2 / 16);
     for (int i = tid; i < n16; i += blockDim.x) dst[i] = src[i];
-    for (int i = tid; i < NP; i += blockDim.x) sVexp[i] = A.vexp[i];
+    const int g1 = A.misc[0] + 1;
+    for (int i = tid; i < NP; i += blockDim.x) {
+      const int e = A.vexp[i];
+      sVexp[i] = e;
+      const int sc = e + g1;
+      sScale[i] = (sc >= -126 && sc <= 127) ? pow2f(sc) : 0.0f;
+    }
   }
   if (tid == 0) {
     for (int i = 0; i < R; ++i) {
@@ -298,18 +318,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_fused(OzArgs A) {
   const int64_t t_end = npairs * (blockIdx.x + 1) / gridDim.x;
 
   if (warp >= kProdWarp0) {
-    // producer thread: determinant d of the tile pair (consecutive lanes take
-    // consecutive beta columns), quarter qq (pairs 4 qq .. 4 qq + 3) of every
-    // K chunk
+    // producer thread: quarter qq = lane & 3 (pairs 4 qq .. 4 qq + 3 of every
+    // K chunk) of determinant d (a warp takes 8 consecutive beta columns).
+    // The two lanes of a quarter pair (qq, qq ^ 1) swap halves so that each
+    // stores one whole 16-byte core-matrix row per slice: the even lane the
+    // real row 2 dl, the odd lane the imaginary row 2 dl + 1, k = 8 (qq >> 1)
+    // .. + 7.  A warp's 32 rows x 16 bytes then cover every bank four times
+    // (4 wavefronts for 512 bytes, no conflicts).
     const int pt = tid - kProdWarp0 * 32;
-    const int d = pt & 63, qq = pt >> 6;
+    const int qq = lane & 3;
+    const int d = (pt >> 5) * 8 + (lane >> 2);
     const int tile = d >> 5, dl = d & 31;
+    const bool odd = (qq & 1) != 0;
     const uint32_t lenb32 = (uint32_t)A.lenb;
-    // byte offset of this thread's two half rows (real, imaginary) in a
-    // slice region of a slot: tile half, core-matrix row 2 dl, k 4 qq
+    // byte offset of this thread's row in a slice region of a slot
     const uint32_t roff =
         (uint32_t)tile * (uint32_t)kChunkElems * 2u +
-        tc::kmajor_offset(2 * dl, 4 * qq, kChunkK) * 2u;
+        tc::kmajor_offset(2 * dl + (odd ? 1 : 0), 8 * (qq >> 1), kChunkK) * 2u;
     const uint32_t sD0 = tc::smem_u32(sD);
     int slot = 0;
     uint32_t ph = 0;
@@ -324,12 +349,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_fused(OzArgs A) {
       const bool valid = live_tile && ib < lenb32;
       const int4* pa = reinterpret_cast<const int4*>(A.tabTA + (size_t)ia * KP + 4 * qq);
       const int4* pb = reinterpret_cast<const int4*>(A.tabTB + (size_t)ib * KP + 4 * qq);
+      // this quarter's four table entries per spin (one 16-byte load each),
+      // loaded one K chunk ahead so that a chunk's gathers wait for one
+      // global round trip, not two
+      int4 tan = make_int4(0, 0, 0, 0), tbn = tan;
+      if (valid) {
+        tan = __ldg(pa);
+        tbn = __ldg(pb);
+      }
       for (int c = 0; c < nch; ++c) {
-        // this quarter's four table entries per spin: one 16-byte load each
-        int4 ta = make_int4(0, 0, 0, 0), tb = ta;
-        if (valid) {
-          ta = __ldg(pa + 4 * c);
-          tb = __ldg(pb + 4 * c);
+        const int4 ta = tan, tb = tbn;
+        if (valid && c + 1 < nch) {
+          tan = __ldg(pa + 4 * (c + 1));
+          tbn = __ldg(pb + 4 * (c + 1));
         }
         const int32_t cas[4] = {ta.x, ta.y, ta.z, ta.w};
         const int32_t cbs[4] = {tb.x, tb.y, tb.z, tb.w};
@@ -376,12 +408,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_fused(OzArgs A) {
         const uint32_t base = sD0 + (uint32_t)slot * (uint32_t)kSlotBytes + roff;
 #pragma unroll
         for (int k = 0; k < kDSlices; ++k) {
-          // 8 bytes of row 2 dl (real) and 8 of row 2 dl + 1 (imaginary)
+          // the even lane keeps its real half and takes its partner's; the odd
+          // lane keeps its imaginary half, which comes second in the row
+          const uint32_t s0 = odd ? re[k][0] : im[k][0], s1 = odd ? re[k][1] : im[k][1];
+          const uint32_t r0 = __shfl_xor_sync(0xffffffffu, s0, 1);
+          const uint32_t r1 = __shfl_xor_sync(0xffffffffu, s1, 1);
+          const uint32_t w0 = odd ? r0 : re[k][0], w1 = odd ? r1 : re[k][1];
+          const uint32_t w2 = odd ? im[k][0] : r0, w3 = odd ? im[k][1] : r1;
           const uint32_t q = base + (uint32_t)k * (uint32_t)kPairChunkElems * 2u;
-          asm volatile("st.shared.v2.b32 [%0], {%1,%2};" ::"r"(q), "r"(re[k][0]), "r"(re[k][1])
-                       : "memory");
-          asm volatile("st.shared.v2.b32 [%0], {%1,%2};" ::"r"(q + 16u), "r"(im[k][0]),
-                       "r"(im[k][1])
+          asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(q), "r"(w0), "r"(w1),
+                       "r"(w2), "r"(w3)
                        : "memory");
         }
         // generic-proxy writes -> visible to the tensor core (async proxy)
@@ -447,8 +483,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_fused(OzArgs A) {
 #pragma unroll
           for (int a = 1; a <= kSlices; ++a) {
             if (a + b <= kMaxLevel) {
-              const int lvl = a + b;
-              const int ai = lvl <= 4 ? lvl - 2 : 3;
+              const int ai = acc_of(a, b);
               const uint32_t accum = (b == 1 && a <= 4) ? (first ^ 1u) : 1u;
               tc::mma_bf16_if(accs[ai], da, vdesc0[a - 1] + kb, idesc, accum, elect);
             }
@@ -478,7 +513,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_fused(OzArgs A) {
     const int half = row >> 6;                // slice tile of the pair
     const int det = (row & 63) >> 1;          // determinant in that tile
     const int part = row & 1;                 // 0 real, 1 imaginary
-    const int cw = NP / 2;                    // pairs per column half (multiple of 8)
+    const int cw = NP / 2;                    // pairs per column half (NP / 16 * 8)
     const int pbeg = cg * cw;
     const int nst = min(cw, A.P - A.p0 - pbeg);  // columns holding real pairs
     // D = 2^(g0 + 1) sum_b slice_b for every determinant (one global scale)
@@ -503,47 +538,66 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_fused(OzArgs A) {
       // this lane's half of G[p][det]: (hi, lo) of the real or imaginary part
       float2* gp = reinterpret_cast<float2*>(A.G + ia * A.gld + (ib - A.c0)) + part +
                    (int64_t)(A.p0 + pbeg) * pstride;
-      // four columns at a time: the four level sums, combined into an FP32
-      // pair by a chain of exact two-sums (with one global scale a column's
-      // leading bits may sit in level 4 or later, so no level is assumed to
-      // dominate; the rounding errors are summed in l), scaled and stored
-      for (int c0 = 0; c0 < cw; c0 += 4) {
-        const int pc = pbeg + c0;
-        uint32_t ra[4], rb[4], rc[4], rd[4];
-        tc::tmem_ld4_nowait(base + (uint32_t)pc, ra);
-        tc::tmem_ld4_nowait(base + (uint32_t)(NP + pc), rb);
-        tc::tmem_ld4_nowait(base + (uint32_t)(2 * NP + pc), rc);
-        tc::tmem_ld4_nowait(base + (uint32_t)(3 * NP + pc), rd);
-        tc::tmem_wait_ld();
+      // Four columns at a time, software-pipelined: the TMEM loads of the
+      // next four columns are in flight while these are combined and stored.
+      // Per column the four level sums become an FP32 pair (h, l) by a chain
+      // of exact two-sums (with one global scale a column's leading bits may
+      // sit in level 4 or later, so no level is assumed to dominate; the
+      // rounding errors are summed in l).  The pair is left unnormalised: the
+      // scatter adds it in FP32-pair arithmetic, which absorbs l.
+      uint32_t xa[16], xb[16];  // [level * 4 + column]
+      auto load4 = [&](uint32_t (&x)[16], int pc) {
+        uint32_t (&x0)[4] = *reinterpret_cast<uint32_t (*)[4]>(&x[0]);
+        uint32_t (&x1)[4] = *reinterpret_cast<uint32_t (*)[4]>(&x[4]);
+        uint32_t (&x2)[4] = *reinterpret_cast<uint32_t (*)[4]>(&x[8]);
+        uint32_t (&x3)[4] = *reinterpret_cast<uint32_t (*)[4]>(&x[12]);
+        tc::tmem_ld4_nowait(base + (uint32_t)pc, x0);
+        tc::tmem_ld4_nowait(base + (uint32_t)(NP + pc), x1);
+        tc::tmem_ld4_nowait(base + (uint32_t)(2 * NP + pc), x2);
+        tc::tmem_ld4_nowait(base + (uint32_t)(3 * NP + pc), x3);
+      };
+      auto emit4 = [&](const uint32_t (&x)[16], int c0) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          float h, l;
-          two_sum(__uint_as_float(ra[k]), __uint_as_float(rb[k]), h, l);
-          float e2;
-          two_sum(h, __uint_as_float(rc[k]), h, e2);
+          float h, l, e2;
+          two_sum(__uint_as_float(x[k]), __uint_as_float(x[4 + k]), h, l);
+          two_sum(h, __uint_as_float(x[8 + k]), h, e2);
           l += e2;
-          two_sum(h, __uint_as_float(rd[k]), h, e2);
+          two_sum(h, __uint_as_float(x[12 + k]), h, e2);
           l += e2;
-          const float h2 = h + l;
-          const float l2 = l - (h2 - h);
-          // with the row exponent of V
-          const int sc = sVexp[pc + k] + colexp;
+          const int pc = pbeg + c0 + k;
+          // with the row exponent of V: 2^(eV(p) + g0 + 1), precomputed
+          const float f = sScale[pc];
           float hs, ls;
-          if (sc >= -126 && sc <= 127) {
-            const float f = pow2f(sc);
-            hs = h2 * f;
-            ls = l2 * f;
-          } else {
-            hs = scale2(h2, sc);
-            ls = scale2(l2, sc);
+          if (f != 0.0f) {
+            hs = h * f;
+            ls = l * f;
+          } else {  // outside FP32's normal exponent range: two steps
+            const int sc = sVexp[pc] + colexp;
+            hs = scale2(h, sc);
+            ls = scale2(l, sc);
           }
           if (live && c0 + k < nst) gp[(int64_t)(c0 + k) * pstride] = make_float2(hs, ls);
         }
+      };
+      // cw is a multiple of 8: the batches come in pairs
+      load4(xa, pbeg);
+      for (int c0 = 0; c0 < cw; c0 += 8) {
+        tc::tmem_wait_ld_tied(xa);
+        load4(xb, pbeg + c0 + 4);
+        emit4(xa, c0);
+        tc::tmem_wait_ld_tied(xb);
+        if (c0 + 8 < cw) {
+          load4(xa, pbeg + c0 + 8);
+        } else {
+          // every TMEM load of this warp has completed: release the
+          // accumulators before the last four columns are stored
+          tc::fence_before_sync();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(accempty);
+        }
+        emit4(xb, c0 + 4);
       }
-      // every TMEM load of this warp has completed (wait::ld above): release
-      tc::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(accempty);
     }
   }
   tc::fence_before_sync();
@@ -795,7 +849,7 @@ static bool oz_shape(int P, int smax, int& KP, int& npass, int& NP, size_t& fixe
   NP = ((P + npass - 1) / npass + 15) / 16 * 16;
   if (NP > kM) return false;
   fixed = sizeof(__nv_bfloat16) * (size_t)kSlices * NP * KP +
-          sizeof(uint64_t) * (2 * kMaxRing + 3) + 16 + sizeof(int) * kM;
+          sizeof(uint64_t) * (2 * kMaxRing + 3) + 16 + sizeof(int) * kM + sizeof(float) * kM;
   return fixed + 2 * (size_t)kSlotBytes <= (size_t)smax;
 }
 

@@ -106,8 +106,8 @@ def _two_sum(a, b):
 def combine_chain(acc, e_row, e_col):
     """G from the level sums by a chain of exact two-sums in FP32:
     (s, e) = two-sum(level 2, level 3), then s absorbs level 4 and levels
-    5..7 the same way, the rounding errors summed in e; (s + e) is
-    renormalised and scaled by 2^(e_row + e_col).  Unlike `combine` it does
+    5..7 the same way, the rounding errors summed in e; (s, e) is scaled by
+    2^(e_row + e_col).  Unlike `combine` it does
     not assume that levels 2 and 3 hold the leading bits, which fails when
     D is scaled globally and a column's value starts in level 4 or later."""
     a = [acc[i].astype(numpy.float32) for i in range(4)]
@@ -115,10 +115,10 @@ def combine_chain(acc, e_row, e_col):
     for k in (2, 3):
         s, e2 = _two_sum(s, a[k])
         e = (e + e2).astype(numpy.float32)
-    h = (s + e).astype(numpy.float32)
-    l = (e - (h - s)).astype(numpy.float32)
+    # the pair (s, e) is stored unnormalised; the scatter's FP32-pair sum
+    # takes it as it is
     scale = numpy.ldexp(1.0, e_row[:, None] + e_col[None, :])
-    return (h.astype(numpy.float64) + l.astype(numpy.float64)) * scale
+    return (s.astype(numpy.float64) + e.astype(numpy.float64)) * scale
 
 
 def psi_bound_exponents(psi):
