@@ -555,6 +555,16 @@ def configs_leg():
         row["diag_coulomb_evolve"] = {
             "ms": t_dc, "gbs": 32.0 * n / (t_dc / 1e3) / 1e9,
             "norm_after_11_steps": float(torch.linalg.norm(w.get_coeff(key)))}
+        # one- and two-particle RDMs of the sector (FqeData.rdm12): the
+        # dvecs' Gram matrix streamed by k_rdm2_gram, norb^4 N complex MACs
+        # in FP64 over the Hermitian half
+        d = w._civec[key]
+        d.rdm12()
+        _, t_r12 = timed(lambda: d.rdm12())
+        _, t_r1 = timed(lambda: d.rdm1(), 3)
+        p = norb * norb
+        row["rdm"] = {"rdm1_ms": t_r1, "rdm12_ms": t_r12,
+                      "rdm12_fp64_tflops": 8.0 * p * (p + 1) / 2 * n / (t_r12 / 1e3) / 1e12}
         out["norb14"] = row
     finally:
         settings.precision = old

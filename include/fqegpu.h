@@ -388,10 +388,10 @@ int fqegpu_mlp_adam(fqegpu_mlp m, double lr, double beta1, double beta2,
 /* ---- test hooks (no counterpart in the reference) --------------------------
  * Failure detection is tested without a GPU fault: the tensor-core kernel's
  * bounded waits give up after `wait_cycles` clock cycles (<= 0: the default,
- * about 2 s) and, with skip_slot >= 0, the loader of its first CTA leaves that
- * ring slot of its first tile pair unfilled, so the consumer's wait runs out
- * and the apply reports FQEGPU_ERR_TIMEOUT (the kernel waits for its issued
- * copies and frees its tensor memory before it exits).  skip_slot = -1 and
+ * about 2 s) and, with skip_slot >= 0, the producers of its first CTA leave
+ * that ring slot of its first tile pair unfilled, so the MMA warp's wait runs
+ * out and the apply reports FQEGPU_ERR_TIMEOUT (the kernel waits for the MMAs
+ * it issued and frees its tensor memory before it exits).  skip_slot = -1 and
  * wait_cycles = 0 restore normal operation.  fqegpu_debug_fail_allocs makes
  * the library's next `count` device allocations fail as on an exhausted
  * device (FQEGPU_ERR_NOMEM). */

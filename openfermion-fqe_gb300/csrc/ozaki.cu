@@ -122,7 +122,7 @@ struct OzakiPlan {
   cudaEvent_t err_ev = nullptr;
   bool err_pending = false;
   // bounded-wait limit (clock cycles) and a test-only fault injection: when
-  // skip_slot >= 0 the loader of CTA 0 leaves that ring slot of its first
+  // skip_slot >= 0 the producers of CTA 0 leave that ring slot of its first
   // tile pair unfilled, so the MMA warp's wait on it must run out
   long long wait_cycles = kWaitCycles;
   int skip_slot = -1;

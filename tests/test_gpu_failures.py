@@ -5,9 +5,9 @@ lib/macros.c:25-46) and has no device waits.  Here every failure becomes a
 status code and the context stays usable:
 
 * a bounded wait of the tensor-core kernel runs out: a test hook shortens the
-  wait limit and makes the loader of one CTA leave one ring slot unfilled (a
+  wait limit and makes the producers of one CTA leave one ring slot unfilled (a
   flag that nothing sets), so the MMA warp's wait gives up; the kernel waits
-  for the copies it issued, frees its tensor memory and returns; the handle
+  for the MMAs it issued, frees its tensor memory and returns; the handle
   reports FQEGPU_ERR_TIMEOUT (TimeoutError) and the next normal apply is
   correct;
 * device allocations fail as on an exhausted device (fqegpu_debug_fail_allocs):
