@@ -318,16 +318,17 @@ __global__ void __launch_bounds__(kRegWarps * 32, 1) k_oz_fused(OzArgs A) {
   const int64_t t_end = npairs * (blockIdx.x + 1) / gridDim.x;
 
   if (warp >= kProdWarp0) {
-    // producer thread: quarter qq = lane & 3 (pairs 4 qq .. 4 qq + 3 of every
-    // K chunk) of determinant d (a warp takes 8 consecutive beta columns).
-    // The two lanes of a quarter pair (qq, qq ^ 1) swap halves so that each
-    // stores one whole 16-byte core-matrix row per slice: the even lane the
-    // real row 2 dl, the odd lane the imaginary row 2 dl + 1, k = 8 (qq >> 1)
-    // .. + 7.  A warp's 32 rows x 16 bytes then cover every bank four times
-    // (4 wavefronts for 512 bytes, no conflicts).
+    // producer thread: quarter qq (pairs 4 qq .. 4 qq + 3 of every K chunk)
+    // of determinant d; a warp takes 8 consecutive beta columns.  The two
+    // lanes of a quarter pair (qq, qq ^ 1; adjacent lanes) swap halves so
+    // that each stores one whole 16-byte core-matrix row per slice: the even
+    // lane the real row 2 dl, the odd lane the imaginary row 2 dl + 1, k =
+    // 8 (qq >> 1) .. + 7.  Lane bits (qq & 1, d & 3, qq >> 1, d >> 2 of the
+    // warp's 8) put rows 0..7 of one K core in every 8-lane phase of a
+    // 16-byte store: 128 contiguous bytes, no bank conflicts.
     const int pt = tid - kProdWarp0 * 32;
-    const int qq = lane & 3;
-    const int d = (pt >> 5) * 8 + (lane >> 2);
+    const int qq = ((lane >> 3) & 1) * 2 + (lane & 1);
+    const int d = (pt >> 5) * 8 + (lane >> 4) * 4 + ((lane >> 1) & 3);
     const int tile = d >> 5, dl = d & 31;
     const bool odd = (qq & 1) != 0;
     const uint32_t lenb32 = (uint32_t)A.lenb;
