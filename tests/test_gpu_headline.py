@@ -122,3 +122,43 @@ def test_norb16_tensor_core_matches_fp64(gpu):
                 torch.linalg.norm(res["fp64"]))
     print(f"norb 16 (8,8) tensor-core vs FP64 GPU apply: {err:.3e}")
     assert err < TOL_OZ
+
+
+def test_twenty_taylor_steps_norm_and_fidelity(gpu):
+    """The 20-step evolution of the benchmark's norb-16 configuration (dt =
+    0.05, accuracy 1e-12, Wavefunction.apply_generated_unitary 'taylor',
+    wavefunction.py:553-568), at norb 12 (6a,6b) so that the FP64 path can
+    follow every step: on the tensor cores the norm stays within 1e-9 of 1
+    over the 20 steps, the first step's fidelity |<psi_oz|psi_fp64>|^2 is
+    within 1e-10 of 1 and its relative difference below 1e-10, and after 20
+    steps the two trajectories still agree to 1e-9."""
+    import torch
+    from fqe_gb300 import settings, synthetic
+    norb, na, nb = 12, 6, 6
+    h1, h2, psi = synthetic.sector(norb, na, nb, synthetic.default_nchol(norb), 0)
+    ham = gpu.RestrictedHamiltonian((h1, h2))
+    key = (na + nb, na - nb)
+    old = settings.precision
+    traj = {}
+    try:
+        for prec in ("ozaki", "fp64"):
+            settings.precision = prec
+            w = gpu.Wavefunction([[na + nb, na - nb, norb]])
+            w.set_wfn(strategy="from_data", raw_data={key: psi})
+            states = []
+            for _ in range(20):
+                w = w.apply_generated_unitary(0.05, "taylor", ham, accuracy=1e-12,
+                                              expansion=80)
+                states.append(w.get_coeff(key).clone())
+            traj[prec] = states
+    finally:
+        settings.precision = old
+    oz, f64 = traj["ozaki"], traj["fp64"]
+    for s in oz:
+        assert abs(float(torch.linalg.norm(s)) - 1.0) < 1e-9
+    a, b = oz[0].reshape(-1), f64[0].reshape(-1)
+    fid = abs(complex(torch.vdot(a, b))) ** 2 / (float(torch.linalg.norm(a)) ** 2 *
+                                                 float(torch.linalg.norm(b)) ** 2)
+    assert 1.0 - fid < 1e-10
+    assert float(torch.linalg.norm(a - b) / torch.linalg.norm(b)) < 1e-10
+    assert float(torch.linalg.norm(oz[-1] - f64[-1]) / torch.linalg.norm(f64[-1])) < 1e-9

@@ -16,10 +16,11 @@ TOL = 1e-12
 
 
 def _noalloc(lib, norb, na, nb, h1, h2, psi_t, out_t, alpha=1.0, beta=0.0):
-    h1c = numpy.ascontiguousarray(h1, dtype=numpy.complex128)
+    h1c = None if h1 is None else numpy.ascontiguousarray(h1, dtype=numpy.complex128)
     h2c = numpy.ascontiguousarray(h2, dtype=numpy.complex128)
     a, b = complex(alpha), complex(beta)
-    return lib.fqegpu_apply_noalloc(norb, na, nb, h1c.ctypes.data_as(ctypes.c_void_p),
+    p1 = None if h1c is None else h1c.ctypes.data_as(ctypes.c_void_p)
+    return lib.fqegpu_apply_noalloc(norb, na, nb, p1,
                                     h2c.ctypes.data_as(ctypes.c_void_p),
                                     ctypes.c_void_p(psi_t.data_ptr()),
                                     ctypes.c_void_p(out_t.data_ptr()),
@@ -44,6 +45,40 @@ def test_noalloc_matches_apply_twice(gpu, norb, na, nb):
         torch.cuda.synchronize()
         o = out.cpu().numpy()
         assert numpy.linalg.norm(o - ref) / numpy.linalg.norm(ref) < TOL
+
+
+@pytest.mark.parametrize("kind", ["complex", "nonsym", "no_h1", "zero"])
+def test_noalloc_other_operators(gpu, kind):
+    """The uncompressed pair space (complex or non-symmetric integrals,
+    P = norb^2), h1 = NULL, and the zero operator (sigma = beta psi), each
+    against fqegpu_apply on the same inputs."""
+    import torch
+    from fqe_gb300 import _lib, synthetic
+    from fqe_gb300.fqe_data import ham_for
+    lib = _lib.load()
+    norb, na, nb = 7, 3, 4
+    rng = numpy.random.default_rng(7)
+    if kind in ("complex", "nonsym"):
+        h1 = rng.normal(size=(norb,) * 2) + 1j * rng.normal(size=(norb,) * 2)
+        h2 = rng.normal(size=(norb,) * 4) + 1j * rng.normal(size=(norb,) * 4)
+        if kind == "nonsym":
+            h1, h2 = h1.real, h2.real
+    else:
+        h1, h2, _ = synthetic.integrals(norb, norb + 2, 3)
+        if kind == "zero":
+            h1, h2 = numpy.zeros_like(h1), numpy.zeros_like(h2)
+    d = gpu.FqeData(na, nb, norb)
+    d.set_wfn(strategy="from_data",
+              raw_data=synthetic.wavefunction_coeff(d.lena(), d.lenb(), rng))
+    h1_ref = numpy.zeros((norb, norb)) if kind == "no_h1" else h1
+    ref = d._run_apply(ham_for(d._core, h1_ref, h2), 0.5 - 0.25j, 0.75).cpu().numpy()
+    out = torch.full_like(d.coeff, complex("nan"))
+    rc = _noalloc(lib, norb, na, nb, None if kind == "no_h1" else h1, h2, d.coeff, out,
+                  0.5 - 0.25j, 0.75)
+    assert rc == _lib.OK, _lib.last_error()
+    torch.cuda.synchronize()
+    o = out.cpu().numpy()
+    assert numpy.linalg.norm(o - ref) / numpy.linalg.norm(ref) < TOL
 
 
 def test_noalloc_rejects_oversized_sector(gpu):
