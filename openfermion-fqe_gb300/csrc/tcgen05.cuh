@@ -185,35 +185,14 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 
 namespace fqegpu {
 namespace tc {
-// tcgen05.ld of 32 lanes x 16 columns without the wait: several loads can be
-// in flight; tmem_wait_ld() waits for all of them.
-__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-        "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
-        "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-}
-// 32 lanes x 4 columns, no wait.
+// tcgen05.ld of 32 lanes x 4 columns without the wait: several loads can be
+// in flight; tmem_wait_ld_tied() waits for all of them.
 __device__ __forceinline__ void tmem_ld4_nowait(uint32_t taddr, uint32_t (&r)[4]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(taddr));
 }
-// 32 lanes x 8 columns, no wait.
-__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7])
-      : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_wait_ld() {
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-// The same wait, with the destination registers of the loads it completes
+// tcgen05.wait::ld, with the destination registers of the loads it completes
 // tied to it, so that no use of them is scheduled before it.
 __device__ __forceinline__ void tmem_wait_ld_tied(uint32_t (&r)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;"
