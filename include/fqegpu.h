@@ -167,8 +167,10 @@ int fqegpu_apply(fqegpu_ham h, const double *d_psi, double *d_sigma,
 int fqegpu_ham_check(fqegpu_ham h, void *stream);
 /* Same with host buffers: copies psi in and sigma out (pageable or pinned),
  * synchronous; the device staging buffer is allocated on the first call and
- * kept by the handle.  This is the call a ctypes binding inside the
- * reference's FqeData would make. */
+ * kept by the handle.  On the tensor-core path the last scatter runs in row
+ * chunks and each chunk of sigma is copied out (on a copy stream the handle
+ * keeps) while later chunks are scattered.  This is the call a ctypes
+ * binding inside the reference's FqeData would make. */
 int fqegpu_apply_host(fqegpu_ham h, const double *h_psi, double *h_sigma,
                       double alpha_re, double alpha_im, double beta_re,
                       double beta_im, int precision);

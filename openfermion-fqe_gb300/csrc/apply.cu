@@ -642,6 +642,9 @@ static void ham_free(fqegpu_ham h) {
   taylor_destroy(h);
   ozaki_destroy(h);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->out_ev)
+    if (e) cudaEventDestroy(e);
+  if (h->out_stream) cudaStreamDestroy(h->out_stream);
   cudaFree(h->d_Vr);
   cudaFree(h->d_Vc);
   cudaFree(h->d_h1r);
@@ -768,13 +771,36 @@ extern "C" int fqegpu_apply_host(fqegpu_ham h, const double* h_psi,
   // the apply
   if (!h->d_vec) FQE_CUDA(dev_alloc(&h->d_vec, sizeof(double2) * 2 * (size_t)N));
   double2* d = h->d_vec;
+  // the tensor-core path copies sigma out in row chunks on a copy stream of
+  // the handle, behind the scatter of each chunk
+  HostOut ho;
+  if (precision == FQEGPU_PREC_OZAKI) {
+    if (!h->out_stream) {
+      FQE_CUDA(cudaStreamCreateWithFlags(&h->out_stream, cudaStreamNonBlocking));
+      for (int k = 0; k < kOutChunks; ++k)
+        FQE_CUDA(cudaEventCreateWithFlags(&h->out_ev[k], cudaEventDisableTiming));
+    }
+    ho.h_sigma = reinterpret_cast<double2*>(h_sigma);
+    ho.copy = h->out_stream;
+    ho.ev = h->out_ev;
+  }
   int s = FQEGPU_OK;
   cudaError_t e = cudaMemcpy(d, h_psi, sizeof(double2) * N, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {
-    s = fqegpu_apply(h, (const double*)d, (double*)(d + N), alpha_re, alpha_im,
-                     beta_re, beta_im, precision, nullptr);
-    if (s == FQEGPU_OK)
+    if (precision == FQEGPU_PREC_OZAKI) {
+      clear_error();
+      s = apply_ozaki(h, d, d + N, make_double2(alpha_re, alpha_im),
+                      make_double2(beta_re, beta_im), nullptr, &ho);
+    } else {
+      s = fqegpu_apply(h, (const double*)d, (double*)(d + N), alpha_re, alpha_im,
+                       beta_re, beta_im, precision, nullptr);
+    }
+    if (ho.issued) {
+      const cudaError_t e2 = cudaStreamSynchronize(h->out_stream);
+      if (s == FQEGPU_OK) e = e2;
+    } else if (s == FQEGPU_OK) {
       e = cudaMemcpy(h_sigma, d + N, sizeof(double2) * N, cudaMemcpyDeviceToHost);
+    }
   }
   if (e != cudaSuccess) {
     set_error("apply_host: %s", cudaGetErrorString(e));

@@ -97,6 +97,10 @@ struct fqegpu_ham_s {
   // handle's workspace and plan pointers; while nonzero the handle refuses to
   // reallocate them (scratch-limit changes) and to be destroyed.
   int live_graphs = 0;
+  // fqegpu_apply_host: a copy stream and one event per row chunk, so sigma's
+  // finished rows travel to the host while the scatter of later rows runs.
+  cudaStream_t out_stream = nullptr;
+  cudaEvent_t out_ev[8] = {};
 };
 
 namespace fqegpu {
@@ -114,8 +118,19 @@ inline double2 zmul_host(double2 a, double2 b) {
 int stage_mark(fqegpu_ham h, int blk, int k, cudaStream_t st);
 int apply_fp64(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
                double2 beta, cudaStream_t st);
+// Host output of an apply (fqegpu_apply_host): when `h_sigma` is set, the
+// tensor-core path scatters its last beta-column block in row chunks and
+// copies each chunk of sigma to h_sigma on `copy` as soon as it is final
+// (`issued` reports that it did; the caller then waits for `copy`).
+struct HostOut {
+  double2* h_sigma = nullptr;
+  cudaStream_t copy = nullptr;
+  cudaEvent_t* ev = nullptr;  // kOutChunks events
+  bool issued = false;
+};
+constexpr int kOutChunks = 8;
 int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
-                double2 beta, cudaStream_t st);
+                double2 beta, cudaStream_t st, HostOut* out = nullptr);
 void ozaki_destroy(fqegpu_ham h);
 // Creates the tensor-core plan if the operator fits it (FQEGPU_ERR_UNSUPPORTED
 // otherwise: the apply then runs the FP64 kernels).

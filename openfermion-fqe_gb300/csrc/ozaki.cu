@@ -726,8 +726,8 @@ __global__ void __launch_bounds__(256) k_oz_scatter_csr(
     const int32_t* __restrict__ tabA, const int32_t* __restrict__ boff,
     const int2* __restrict__ bent, const float4* __restrict__ G,
     const double2* __restrict__ psi, double2 alpha, double2 beta, int init,
-    const int32_t* __restrict__ misc, double2* __restrict__ sigma) {
-  const int64_t a = blockIdx.y;
+    const int32_t* __restrict__ misc, double2* __restrict__ sigma, int64_t a0) {
+  const int64_t a = a0 + blockIdx.y;
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= lenb) return;
   if (misc[2]) {  // psi holds Inf or NaN
@@ -781,8 +781,8 @@ __global__ void __launch_bounds__(256) k_oz_scatter(
     const int32_t* __restrict__ tabA,
     const int32_t* __restrict__ tabB, const float4* __restrict__ G,
     const double2* __restrict__ psi, double2 alpha, double2 beta, int init,
-    const int32_t* __restrict__ misc, double2* __restrict__ sigma) {
-  const int64_t a = blockIdx.y;
+    const int32_t* __restrict__ misc, double2* __restrict__ sigma, int64_t a0) {
+  const int64_t a = a0 + blockIdx.y;
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= lenb) return;
   if (misc[2]) {  // psi holds Inf or NaN
@@ -1068,7 +1068,7 @@ void ozaki_destroy(fqegpu_ham h) {
 }
 
 int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
-                double2 beta, cudaStream_t st) {
+                double2 beta, cudaStream_t st, HostOut* out) {
   // The split needs a real pair matrix whose shape fits the kernels (P <= 192,
   // shared memory); other operators run the FP64 kernels on the GPU.
   if (h->zero || h->onebody || !h->real || h->P > 192)
@@ -1136,16 +1136,32 @@ int apply_ozaki(fqegpu_ham h, const double2* psi, double2* sigma, double2 alpha,
       FQE_CUDA(cudaGetLastError());
     }
     FQE_TRY(stage_mark(h, blk, 2, st));
-    dim3 sg((unsigned)((lenb + 255) / 256), (unsigned)lena);
-    if (pl->d_boff)
-      k_oz_scatter_csr<<<sg, 256, 0, st>>>(pl->P, lena, lenb, c0, w, pl->wb, tabA,
-                                           pl->d_boff + (size_t)blk * (lenb + 1), pl->d_bent,
-                                           pl->d_G, psi, al, beta, blk == 0 ? 1 : 0,
-                                           pl->d_misc, sigma);
-    else
-      k_oz_scatter<<<sg, 256, 0, st>>>(pl->P, lena, lenb, c0, w, pl->wb, tabA, tabB, pl->d_G,
-                                       psi, al, beta, blk == 0 ? 1 : 0, pl->d_misc, sigma);
-    FQE_CUDA(cudaGetLastError());
+    // the last block's scatter leaves sigma final: with a host output it runs
+    // in row chunks, each copied out as soon as it is written
+    const bool last = c0 + pl->wb >= lenb;
+    const int nchunk = (out && out->h_sigma && last) ? (int)std::min<int64_t>(kOutChunks, lena) : 1;
+    for (int k = 0; k < nchunk; ++k) {
+      const int64_t a0 = lena * k / nchunk, a1 = lena * (k + 1) / nchunk;
+      dim3 sg((unsigned)((lenb + 255) / 256), (unsigned)(a1 - a0));
+      if (pl->d_boff)
+        k_oz_scatter_csr<<<sg, 256, 0, st>>>(pl->P, lena, lenb, c0, w, pl->wb, tabA,
+                                             pl->d_boff + (size_t)blk * (lenb + 1), pl->d_bent,
+                                             pl->d_G, psi, al, beta, blk == 0 ? 1 : 0,
+                                             pl->d_misc, sigma, a0);
+      else
+        k_oz_scatter<<<sg, 256, 0, st>>>(pl->P, lena, lenb, c0, w, pl->wb, tabA, tabB,
+                                         pl->d_G, psi, al, beta, blk == 0 ? 1 : 0, pl->d_misc,
+                                         sigma, a0);
+      FQE_CUDA(cudaGetLastError());
+      if (nchunk > 1) {
+        FQE_CUDA(cudaEventRecord(out->ev[k], st));
+        FQE_CUDA(cudaStreamWaitEvent(out->copy, out->ev[k], 0));
+        FQE_CUDA(cudaMemcpyAsync(out->h_sigma + a0 * lenb, sigma + a0 * lenb,
+                                 sizeof(double2) * (size_t)((a1 - a0) * lenb),
+                                 cudaMemcpyDeviceToHost, out->copy));
+        out->issued = true;
+      }
+    }
     FQE_TRY(stage_mark(h, blk, 3, st));
   }
   if (h->defer_check) return FQEGPU_OK;  // recorded into a graph: checked by its owner

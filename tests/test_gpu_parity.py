@@ -12,6 +12,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 TOL_FP64 = 1e-12
+TOL_OZ = 1e-10
 
 
 def _rel(a, b):
@@ -291,6 +292,29 @@ def test_apply_host_entry_point(gpu, oracle):
     _lib.call("fqegpu_apply_host", ham.handle, psi.ctypes.data_as(ctypes.c_void_p),
               out.ctypes.data_as(ctypes.c_void_p), 1.0, 0.0, 0.0, 0.0, 0)
     assert _rel(out, oracle.apply_spatial12(psi, h1, h2, g)) < TOL_FP64
+
+
+@pytest.mark.parametrize("blocked", [False, True])
+def test_apply_host_tensor_cores(gpu, oracle, blocked):
+    """fqegpu_apply_host on the tensor-core path, whose last scatter runs in
+    row chunks with sigma copied out behind it (pageable numpy buffers), in
+    one block and in beta-column blocks (a small scratch limit); twice, so
+    the handle's copy stream is reused."""
+    from fqe_gb300 import synthetic, _lib
+    from fqe_gb300.fqe_data import _Ham
+    norb, na, nb = 10, 5, 5
+    h1, h2, rng = synthetic.integrals(norb, 20, 3)
+    g = oracle.graph(norb, na, nb)
+    psi = synthetic.wavefunction_coeff(g.lena, g.lenb, rng)
+    ham = _Ham(gpu.FciGraph(na, nb, norb), h1, h2)
+    if blocked:
+        _lib.call("fqegpu_ham_set_scratch_limit", ham.handle, 8 << 20)  # 32-column blocks
+    want = 0.5 * oracle.apply_spatial12(psi, h1, h2, g) - 0.25j * psi
+    for _ in range(2):
+        out = numpy.full_like(psi, numpy.nan)
+        _lib.call("fqegpu_apply_host", ham.handle, psi.ctypes.data_as(ctypes.c_void_p),
+                  out.ctypes.data_as(ctypes.c_void_p), 0.5, 0.0, 0.0, -0.25, 1)
+        assert _rel(out, want) < TOL_OZ
 
 
 def test_apply_rejects_aliasing_and_bad_precision(gpu):
