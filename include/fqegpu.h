@@ -240,8 +240,11 @@ int fqegpu_block_axpy(int64_t n, int k, const double *h_coef,
  * No counterpart in the reference (Wavefunction._apply_array applies sectors
  * one at a time, wavefunction.py:366-399).  Records n applies
  *   d_sigmas[i] = alpha * (H_i d_psis[i]) + beta * d_psis[i]
- * (hams may repeat; they run in order on one stream) into one CUDA graph after
- * one uncaptured pass that allocates every workspace and tensor-core plan.
+ * into one CUDA graph after one uncaptured pass that allocates every
+ * workspace and tensor-core plan.  hams may repeat: the applies of one handle
+ * run in order on one of up to eight parallel branches of the graph, and
+ * applies of different handles may run concurrently, so no sigma may overlap
+ * another entry's psi or sigma (FQEGPU_ERR_INVALID).
  * fqegpu_batch_launch replays the batch with one graph launch (asynchronous);
  * fqegpu_batch_check synchronises `stream` and reports a tensor-core timeout
  * of the last launch.  Buffers are those given at creation.  While a batch

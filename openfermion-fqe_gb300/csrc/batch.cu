@@ -5,9 +5,10 @@
 // each call a separate native invocation.  For many small wavefunctions the
 // launch and synchronisation overhead of one apply at a time dominates, so
 // fqegpu_batch_create runs every (Hamiltonian, psi, sigma) apply once (which
-// allocates workspaces and tensor-core plans), then records all of them, in
-// order, on one stream into a CUDA graph; fqegpu_batch_launch replays the
-// whole batch with one launch.  Buffers are fixed at creation (update their
+// allocates workspaces and tensor-core plans), then records all of them into
+// a CUDA graph of up to eight parallel branches (the applies of one handle in
+// order on one branch); fqegpu_batch_launch replays the whole batch with one
+// launch.  Buffers are fixed at creation (update their
 // contents between launches).  The tensor-core path's end-of-apply error
 // readback is deferred to fqegpu_batch_check.
 #include <algorithm>
@@ -30,6 +31,8 @@ struct fqegpu_batch_s {
 using namespace fqegpu;
 
 namespace {
+
+constexpr int kLanes = 8;  // parallel branches of a batch graph
 
 int apply_one(fqegpu_ham h, const double* psi, double* sigma, double2 al, double2 be,
               int precision, cudaStream_t st) {
@@ -76,6 +79,26 @@ extern "C" int fqegpu_batch_create(int n, const fqegpu_ham* hams, const double* 
     FQE_CHECK_ARG((const void*)d_psis[i] != (const void*)d_sigmas[i],
                   "psi and sigma must not alias");
   }
+  // entries may run concurrently: a sigma must not overlap another entry's
+  // psi or sigma
+  {
+    auto span = [&](int i, const void* p) {
+      const int64_t N = hams[i]->g->a.len * hams[i]->g->b.len;
+      const char* c = static_cast<const char*>(p);
+      return std::make_pair(c, c + sizeof(double2) * (size_t)N);
+    };
+    for (int i = 0; i < n; ++i) {
+      const auto si = span(i, d_sigmas[i]);
+      for (int j = 0; j < n; ++j) {
+        if (j == i) continue;
+        const auto pj = span(j, d_psis[j]), sj = span(j, d_sigmas[j]);
+        FQE_CHECK_ARG(si.second <= pj.first || pj.second <= si.first,
+                      "a sigma of the batch overlaps another entry's psi");
+        FQE_CHECK_ARG(si.second <= sj.first || sj.second <= si.first,
+                      "two sigmas of the batch overlap");
+      }
+    }
+  }
   const double2 al = make_double2(alpha_re, alpha_im), be = make_double2(beta_re, beta_im);
   cudaStream_t st = (cudaStream_t)stream;
   // one uncaptured pass: workspaces, plans and tables exist afterwards
@@ -84,29 +107,61 @@ extern "C" int fqegpu_batch_create(int n, const fqegpu_ham* hams, const double* 
   auto* b = new fqegpu_batch_s();
   b->precision = precision;
   b->hams.assign(hams, hams + n);
-  cudaStream_t cs = nullptr;
-  cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  // Parallel branches: every handle is given one of up to kLanes lanes (its
+  // first appearance, round robin), and its applies run in order on that
+  // lane — a handle's workspace is never used by two branches at once —
+  // while small sectors of different handles run side by side.
+  const std::vector<fqegpu_ham> hs = distinct(b->hams);
+  const int lanes = std::min<int>(kLanes, (int)hs.size());
+  std::vector<int> lane_of(n);
+  for (int i = 0; i < n; ++i)
+    lane_of[i] = (int)(std::find(hs.begin(), hs.end(), hams[i]) - hs.begin()) % lanes;
+  cudaStream_t cs[kLanes] = {};
+  cudaEvent_t fork = nullptr, joins[kLanes] = {};
+  cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+  for (int l = 0; l < lanes && e == cudaSuccess; ++l) {
+    e = cudaStreamCreateWithFlags(&cs[l], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&joins[l], cudaEventDisableTiming);
+  }
   int s = FQEGPU_OK;
   if (e == cudaSuccess) {
-    for (int i = 0; i < n; ++i) hams[i]->defer_check = true;
-    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) {
-      for (int i = 0; i < n && s == FQEGPU_OK; ++i)
-        s = apply_one(hams[i], d_psis[i], d_sigmas[i], al, be, precision, cs);
-      cudaGraph_t g = nullptr;
-      const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
-      b->graph = g;
-      if (e2 != cudaSuccess && s == FQEGPU_OK) e = e2;
+    std::vector<bool> timing(n);
+    for (int i = 0; i < n; ++i) {
+      timing[i] = hams[i]->timing;
+      hams[i]->timing = false;
+      hams[i]->defer_check = true;
     }
-    for (int i = 0; i < n; ++i) hams[i]->defer_check = false;
+    e = cudaStreamBeginCapture(cs[0], cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      e = cudaEventRecord(fork, cs[0]);
+      for (int l = 1; l < lanes && e == cudaSuccess; ++l) e = cudaStreamWaitEvent(cs[l], fork, 0);
+      for (int i = 0; i < n && s == FQEGPU_OK && e == cudaSuccess; ++i)
+        s = apply_one(hams[i], d_psis[i], d_sigmas[i], al, be, precision, cs[lane_of[i]]);
+      for (int l = 1; l < lanes && e == cudaSuccess && s == FQEGPU_OK; ++l) {
+        e = cudaEventRecord(joins[l], cs[l]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(cs[0], joins[l], 0);
+      }
+      cudaGraph_t g = nullptr;
+      const cudaError_t e2 = cudaStreamEndCapture(cs[0], &g);
+      b->graph = g;
+      if (e2 != cudaSuccess && s == FQEGPU_OK && e == cudaSuccess) e = e2;
+    }
+    for (int i = 0; i < n; ++i) {
+      hams[i]->defer_check = false;
+      hams[i]->timing = timing[i];
+    }
     if (e == cudaSuccess && s == FQEGPU_OK) {
       e = cudaGraphInstantiate(&b->exec, b->graph, 0);
       if (e != cudaSuccess) b->exec = nullptr;
     }
     if (b->exec)
-      for (fqegpu_ham h : distinct(b->hams)) ++h->live_graphs;
-    cudaStreamDestroy(cs);
+      for (fqegpu_ham h : hs) ++h->live_graphs;
   }
+  for (int l = 0; l < kLanes; ++l) {
+    if (cs[l]) cudaStreamDestroy(cs[l]);
+    if (joins[l]) cudaEventDestroy(joins[l]);
+  }
+  if (fork) cudaEventDestroy(fork);
   if (s != FQEGPU_OK || e != cudaSuccess) {
     if (s == FQEGPU_OK) {
       set_error("batch capture: %s", cudaGetErrorString(e));
@@ -140,10 +195,6 @@ extern "C" int fqegpu_batch_check(fqegpu_batch b, void* stream) {
 // conditional node whose body is one order); the sectors are spread over
 // kLanes parallel branches of the graph, so small sectors overlap on the GPU.
 // The handles must be distinct (each series uses its handle's work vectors).
-
-namespace {
-constexpr int kLanes = 8;
-}
 
 extern "C" int fqegpu_batch_taylor_create(int n, const fqegpu_ham* hams, double* const* d_psis,
                                           double time, double accuracy, int expansion,

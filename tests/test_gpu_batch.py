@@ -102,3 +102,54 @@ def test_autotuned_batch_matches_fixed(gpu, oracle):
         for s in (s0, s1):
             got = s.cpu().numpy()
             assert numpy.linalg.norm(got - want) / numpy.linalg.norm(want) < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+def test_batch_repeated_handle_and_overlap(gpu, precision):
+    """Through the C ABI: one handle used by three entries (its applies share
+    the handle's workspace, so they stay in order on one branch of the graph)
+    beside a second handle; results bit-identical to single applies.  A sigma
+    that overlaps another entry's psi is refused (the entries may run
+    concurrently)."""
+    import ctypes
+    import torch
+    from fqe_gb300 import _lib, synthetic
+    from fqe_gb300.fqe_data import _Ham, _ptr
+    code = {"fp64": _lib.PREC_FP64, "ozaki": _lib.PREC_OZAKI}[precision]
+    norb, na, nb = 10, 5, 5
+    h1, h2, psi = synthetic.sector(norb, na, nb, 20, seed=5)
+    d = gpu.FqeData(na, nb, norb)
+    d.set_wfn(strategy="from_data", raw_data=psi)
+    e = gpu.FqeData(4, 4, 8)
+    g1, g2, psi_e = synthetic.sector(8, 4, 4, 16, seed=6)
+    e.set_wfn(strategy="from_data", raw_data=psi_e)
+    ha, hb = _Ham(d._core, h1, h2), _Ham(e._core, g1, g2)
+    psis = [d.coeff, d.coeff * (0.5 - 1j), e.coeff, d.coeff.conj()]
+    hams = [ha, ha, hb, ha]
+    sigmas = [torch.empty_like(p) for p in psis]
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def create(sig):
+        n = len(hams)
+        hv = (ctypes.c_void_p * n)(*[h.handle.value for h in hams])
+        pv = (ctypes.c_void_p * n)(*[p.data_ptr() for p in psis])
+        sv = (ctypes.c_void_p * n)(*[s.data_ptr() for s in sig])
+        out = ctypes.c_void_p()
+        _lib.call("fqegpu_batch_create", n, hv, pv, sv, 0.3, 0.1, -0.2, 0.0, code, stream,
+                  ctypes.byref(out))
+        return out
+
+    b = create(sigmas)
+    try:
+        _lib.call("fqegpu_batch_launch", b, stream)
+        _lib.call("fqegpu_batch_check", b, stream)
+        for h, p, s in zip(hams, psis, sigmas):
+            one = torch.empty_like(p)
+            _lib.call("fqegpu_apply", h.handle, _ptr(p), _ptr(one), 0.3, 0.1, -0.2, 0.0, code,
+                      stream)
+            torch.cuda.synchronize()
+            assert torch.equal(one, s)
+    finally:
+        _lib.load().fqegpu_batch_destroy(b)
+    with pytest.raises(ValueError, match="overlaps"):
+        create([sigmas[0], sigmas[1], sigmas[2], psis[1]])
