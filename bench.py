@@ -29,6 +29,7 @@ same line (default sector norb=12 (6a,6b); --davidson-norb, --no-davidson).
                                  the tensor cores, first step against FP64
   python bench.py --no-cpu-baseline --davidson-norb 16 --davidson-scratch-gb 20
                                  Davidson to 1e-6 at norb 16, learned vs plain
+  python bench.py --diag         the norb-14 diagonal-Coulomb evolve, 20 calls
 """
 
 import argparse
@@ -571,6 +572,43 @@ def configs_leg():
     return out
 
 
+def diag_leg(norb=14, calls=20):
+    """The diagonal-Coulomb evolve t = 0.1 of the norb (norb/2, norb/2)
+    sector (V ~ N(0, 0.5) symmetric, seeded), in place, `calls` times (CUDA
+    events on the current stream): time per call, its 32 B/det against the
+    measured copy rate, and the norm afterwards."""
+    import torch
+    import fqe_gb300
+    from fqe_gb300 import settings, synthetic
+    na = nb = norb // 2
+    key = (na + nb, 0)
+    _, _, psi = synthetic.sector(norb, na, nb, synthetic.default_nchol(norb), SEED)
+    w = fqe_gb300.Wavefunction([[na + nb, 0, norb]])
+    w.set_wfn(strategy="from_data", raw_data={key: psi})
+    dc = fqe_gb300.get_diagonalcoulomb_hamiltonian(synthetic.diagonal_coulomb(norb, SEED))
+    old = settings.precision
+    try:
+        settings.precision = "fp64"
+        for _ in range(3):
+            w.time_evolve(0.1, dc, inplace=True)
+        torch.cuda.synchronize()
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(calls):
+            w.time_evolve(0.1, dc, inplace=True)
+        e.record()
+        torch.cuda.synchronize()
+        ms = s.elapsed_time(e) / calls
+    finally:
+        settings.precision = old
+    n = psi.size
+    return {"workload": f"diagonal-Coulomb evolve t=0.1, norb={norb} ({na}a,{nb}b), "
+                        f"{n} determinants, seed {SEED}",
+            "ms": ms, "hbm_gbs": 32.0 * n / (ms / 1e3) / 1e9,
+            "norm_after": float(torch.linalg.norm(w.get_coeff(key)))}
+
+
 def taylor_leg(norb=16, steps=20, dt=0.05, accuracy=1e-12, fp64_check=True):
     """The norb-16 (8a,8b) configuration: `steps` Taylor steps of dt on the
     tensor cores (Ozaki-split BF16), per step the wall time, the number of
@@ -761,6 +799,8 @@ def main():
     ap.add_argument("--taylor16", action="store_true",
                     help="only the norb-16 (8a,8b) 20-step Taylor evolution "
                          "(tensor cores) with the first step against FP64")
+    ap.add_argument("--diag", action="store_true",
+                    help="only the norb-14 diagonal-Coulomb evolve (20 timed calls)")
     ap.add_argument("--configs", action="store_true",
                     help="only measure the other single-GPU configurations "
                          "(norb 8 apply/Taylor; norb 14 FP64 vs tensor-core "
@@ -774,13 +814,15 @@ def main():
                      args.nchol or synthetic.default_nchol(args.norb))
     if args.impl == "reference":
         return run_reference(args)
-    if args.configs or args.taylor16 or args.batch:
+    if args.configs or args.taylor16 or args.batch or args.diag:
         import torch
         import fqe_gb300
         torch.cuda.set_device(0)
         fqe_gb300.build()
         if args.batch:
             print(json.dumps({"batch": batch_leg()}), flush=True)
+        elif args.diag:
+            print(json.dumps({"diag_coulomb": diag_leg()}), flush=True)
         elif args.taylor16:
             print(json.dumps({"taylor_norb16": taylor_leg(
                 fp64_check=not args.no_fp64_check)}), flush=True)
