@@ -30,6 +30,7 @@ same line (default sector norb=12 (6a,6b); --davidson-norb, --no-davidson).
   python bench.py --no-cpu-baseline --davidson-norb 16 --davidson-scratch-gb 20
                                  Davidson to 1e-6 at norb 16, learned vs plain
   python bench.py --diag         the norb-14 diagonal-Coulomb evolve, 20 calls
+  python bench.py --rdm          the norb-14 one- and two-particle RDMs
 """
 
 import argparse
@@ -609,6 +610,41 @@ def diag_leg(norb=14, calls=20):
             "norm_after": float(torch.linalg.norm(w.get_coeff(key)))}
 
 
+def rdm_leg(norb=14):
+    """One- and two-particle RDMs (FqeData.rdm1 / rdm12) of the norb
+    (norb/2, norb/2) sector's seeded wavefunction, CUDA events: rdm1 three
+    times, rdm12 once after a warm-up, and rdm12's FP64 rate on the
+    Hermitian half of its Gram matrix (norb^2 (norb^2 + 1) / 2 complex
+    multiply-adds per determinant)."""
+    import torch
+    import fqe_gb300
+    from fqe_gb300 import synthetic
+    na = nb = norb // 2
+    _, _, psi = synthetic.sector(norb, na, nb, synthetic.default_nchol(norb), SEED)
+    d = fqe_gb300.FqeData(na, nb, norb)
+    d.set_wfn(strategy="from_data", raw_data=psi)
+
+    def timed(fn, reps=1):
+        torch.cuda.synchronize()
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(reps):
+            fn()
+        e.record()
+        torch.cuda.synchronize()
+        return s.elapsed_time(e) / reps
+
+    d.rdm1()
+    t1 = timed(lambda: d.rdm1(), 3)
+    d.rdm12()
+    t12 = timed(lambda: d.rdm12())
+    p, n = norb * norb, psi.size
+    return {"workload": f"rdm1 and rdm12, norb={norb} ({na}a,{nb}b), {n} determinants",
+            "rdm1_ms": t1, "rdm12_ms": t12,
+            "rdm12_fp64_tflops": 8.0 * p * (p + 1) / 2 * n / (t12 / 1e3) / 1e12}
+
+
 def taylor_leg(norb=16, steps=20, dt=0.05, accuracy=1e-12, fp64_check=True):
     """The norb-16 (8a,8b) configuration: `steps` Taylor steps of dt on the
     tensor cores (Ozaki-split BF16), per step the wall time, the number of
@@ -799,6 +835,8 @@ def main():
     ap.add_argument("--taylor16", action="store_true",
                     help="only the norb-16 (8a,8b) 20-step Taylor evolution "
                          "(tensor cores) with the first step against FP64")
+    ap.add_argument("--rdm", action="store_true",
+                    help="only the norb-14 one- and two-particle RDMs")
     ap.add_argument("--diag", action="store_true",
                     help="only the norb-14 diagonal-Coulomb evolve (20 timed calls)")
     ap.add_argument("--configs", action="store_true",
@@ -814,7 +852,7 @@ def main():
                      args.nchol or synthetic.default_nchol(args.norb))
     if args.impl == "reference":
         return run_reference(args)
-    if args.configs or args.taylor16 or args.batch or args.diag:
+    if args.configs or args.taylor16 or args.batch or args.diag or args.rdm:
         import torch
         import fqe_gb300
         torch.cuda.set_device(0)
@@ -823,6 +861,8 @@ def main():
             print(json.dumps({"batch": batch_leg()}), flush=True)
         elif args.diag:
             print(json.dumps({"diag_coulomb": diag_leg()}), flush=True)
+        elif args.rdm:
+            print(json.dumps({"rdm": rdm_leg()}), flush=True)
         elif args.taylor16:
             print(json.dumps({"taylor_norb16": taylor_leg(
                 fp64_check=not args.no_fp64_check)}), flush=True)

@@ -146,7 +146,7 @@ __device__ __forceinline__ double2 dvec_value(int64_t p, int64_t lena, int64_t l
 // grid.x: tiles (tr, tc) in row-major order over ntile x ntile (only
 // tr <= tc when `herm`), grid.y: chunks of sub-blocks.
 __global__ void __launch_bounds__(256) k_rdm2_gram(
-    int P, int ntile, int herm, int64_t lena, int64_t lenb, int64_t nsub_b,
+    int P, int ntile, int E, int herm, int64_t lena, int64_t lenb, int64_t nsub_b,
     const int32_t* __restrict__ tabA, const int32_t* __restrict__ tabB,
     const double2* __restrict__ bra, const double2* __restrict__ ket,
     const int32_t* __restrict__ tiles, double2* __restrict__ partial) {
@@ -163,11 +163,11 @@ __global__ void __launch_bounds__(256) k_rdm2_gram(
   for (int64_t u = u0; u < u1; ++u) {
     const int64_t a = u / nsub_b, b0 = (u - a * nsub_b) * kGSub;
     __syncthreads();
-    for (int idx = threadIdx.x; idx < 2 * kGT * kGSub; idx += blockDim.x) {
-      const int which = idx / (kGT * kGSub);
-      const int pp = (idx / kGSub) % kGT, d = idx % kGSub;
+    for (int idx = threadIdx.x; idx < 2 * E * kGSub; idx += blockDim.x) {
+      const int which = idx / (E * kGSub);
+      const int pp = (idx / kGSub) % E, d = idx % kGSub;
       const int64_t b = b0 + d;
-      const int p = (which ? tc : tr) * kGT + pp;
+      const int p = (which ? tc : tr) * E + pp;
       double2 v = make_double2(0.0, 0.0);
       if (p < P && b < lenb)
         v = dvec_value(p, lena, lenb, a, b, tabA, tabB, which ? ket : bra);
@@ -177,14 +177,18 @@ __global__ void __launch_bounds__(256) k_rdm2_gram(
         sB[pp][d] = v;
     }
     __syncthreads();
+    // rows r >= E (whole warps when E = 28) have no pair: they skip the
+    // multiply-adds; columns >= E read unfilled entries and are never stored
+    if (r < E) {
 #pragma unroll 4
-    for (int d = 0; d < kGSub; ++d) {
-      const double2 x = sB[r][d];  // conj(x) * y
+      for (int d = 0; d < kGSub; ++d) {
+        const double2 x = sB[r][d];  // conj(x) * y
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const double2 y = sK[c0 + i][d];
-        acc[i].x += x.x * y.x + x.y * y.y;
-        acc[i].y += x.x * y.y - x.y * y.x;
+        for (int i = 0; i < 4; ++i) {
+          const double2 y = sK[c0 + i][d];
+          acc[i].x += x.x * y.x + x.y * y.y;
+          acc[i].y += x.x * y.y - x.y * y.x;
+        }
       }
     }
   }
@@ -196,7 +200,7 @@ __global__ void __launch_bounds__(256) k_rdm2_gram(
 
 // raw[P][P] from the partial tiles (fixed chunk order); the lower tiles of
 // a Hermitian Gram are the conjugate transposes of the upper ones.
-__global__ void k_rdm2_final(int P, int ntile, int herm, int ntiles, int nchunk,
+__global__ void k_rdm2_final(int P, int ntile, int E, int herm, int ntiles, int nchunk,
                              const int32_t* __restrict__ tiles,
                              const double2* __restrict__ partial, double2* __restrict__ raw) {
   const int t = blockIdx.x;
@@ -209,8 +213,9 @@ __global__ void k_rdm2_final(int P, int ntile, int herm, int ntiles, int nchunk,
       x += v.x;
       y += v.y;
     }
-    const int i = tr * kGT + e / kGT, j = tc * kGT + e % kGT;
-    if (i < P && j < P) {
+    const int ei = e / kGT, ej = e % kGT;
+    const int i = tr * E + ei, j = tc * E + ej;
+    if (ei < E && ej < E && i < P && j < P) {
       raw[(int64_t)i * P + j] = make_double2(x, y);
       if (herm && tr != tc) raw[(int64_t)j * P + i] = make_double2(x, -y);
     }
@@ -232,6 +237,9 @@ extern "C" int fqegpu_rdm2_gram(fqegpu_graph g, const double* d_bra, const doubl
   const int64_t lena = g->a.len, lenb = g->b.len;
   cudaStream_t st = (cudaStream_t)stream;
   const int ntile = (P + kGT - 1) / kGT;
+  // tile edge: the pairs split evenly over ntile tiles, a multiple of 4 (28
+  // for P = 196, where 32 would pad to 224)
+  const int E = std::min(kGT, ((P + ntile - 1) / ntile + 3) / 4 * 4);
   const int herm = d_bra == d_ket ? 1 : 0;
   std::vector<int32_t> tl;
   for (int tr = 0; tr < ntile; ++tr)
@@ -239,9 +247,25 @@ extern "C" int fqegpu_rdm2_gram(fqegpu_graph g, const double* d_bra, const doubl
   const int ntiles = (int)tl.size();
   const int64_t nsub_b = (lenb + kGSub - 1) / kGSub;
   const int64_t nunits = lena * nsub_b;
-  // about four CTAs per SM in all
-  const int nchunk = (int)std::max<int64_t>(
-      1, std::min<int64_t>(nunits, (4 * kNumSMs + ntiles - 1) / ntiles));
+  // at least four waves of resident CTAs, and a CTA count that fills its
+  // last wave as fully as the chunk choice allows (all CTAs take about the
+  // same time, so a part-filled wave leaves SMs idle at the end)
+  int occ = 1;
+  FQE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_rdm2_gram, 256, 0));
+  const int64_t slots = (int64_t)kNumSMs * std::max(occ, 1);
+  const int64_t cmin = std::max<int64_t>(1, (4 * slots + ntiles - 1) / ntiles);
+  int64_t best = cmin;
+  double best_waste = 2.0;
+  for (int64_t c = cmin; c <= 4 * cmin; ++c) {
+    const int64_t T = c * ntiles, full = (T + slots - 1) / slots * slots;
+    const double waste = (double)(full - T) / (double)full;
+    if (waste < best_waste - 1e-12) {
+      best_waste = waste;
+      best = c;
+    }
+    if (waste < 0.02) break;
+  }
+  const int nchunk = (int)std::max<int64_t>(1, std::min<int64_t>(nunits, best));
   const size_t pbytes = sizeof(double2) * (size_t)nchunk * ntiles * kGT * kGT;
   const size_t rbytes = sizeof(double2) * (size_t)P * P;
   char* scratch = nullptr;
@@ -253,12 +277,13 @@ extern "C" int fqegpu_rdm2_gram(fqegpu_graph g, const double* d_bra, const doubl
                                   cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     k_rdm2_gram<<<dim3(ntiles, nchunk), 256, 0, st>>>(
-        P, ntile, herm, lena, lenb, nsub_b, g->a.tab_full, g->b.tab_full,
+        P, ntile, E, herm, lena, lenb, nsub_b, g->a.tab_full, g->b.tab_full,
         (const double2*)d_bra, (const double2*)d_ket, d_tiles, partial);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    k_rdm2_final<<<ntiles, 256, 0, st>>>(P, ntile, herm, ntiles, nchunk, d_tiles, partial, raw);
+    k_rdm2_final<<<ntiles, 256, 0, st>>>(P, ntile, E, herm, ntiles, nchunk, d_tiles, partial,
+                                         raw);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(h_raw, raw, rbytes, cudaMemcpyDeviceToHost, st);
