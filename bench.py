@@ -62,8 +62,13 @@ UNIT = "det/s"
 # the tensor-core contraction: BF16 slices of D (psi's digits) and products
 OZ_DSLICES, OZ_PRODUCTS = 6, 20
 # DRAM bytes of one k_oz_fused launch over its algorithmic bytes, from the
-# norb-12 ncu capture (profiles/k_oz_fused_norb12.md)
+# norb-12 ncu capture (profiles/k_oz_fused_norb12.md: psi's digit planes fit
+# in L2 there), used for sizes without a capture of their own
 FUSED_TRAFFIC_RATIO = 1.03
+# measured DRAM bytes (read, write) of one k_oz_fused launch by norb for the
+# half-filled sector, one-pass ncu captures of the bench command itself
+# (profiles/k_oz_fused_norb14_dram.md)
+FUSED_TRAFFIC_MEASURED = {14: (13.69e9, 19.74e9)}
 
 
 def peaks():
@@ -356,19 +361,26 @@ def run_gpu(args):
     }
     dk = stages[names[dom]]
     traffic = None
+    traffic_src = None
     if prec == "ozaki" and names[dom] == "contraction":
-        # k_oz_fused DRAM bytes per launch: the full ncu capture of the same
-        # kernel at norb 12 (profiles/k_oz_fused_norb12.md) measured
-        # FUSED_TRAFFIC_RATIO x its algorithmic bytes (psi's digit words read
-        # once, G written once); scaled to this workload's algorithmic bytes
-        traffic = FUSED_TRAFFIC_RATIO * (24.0 * n + 16.0 * P * n)
+        # k_oz_fused DRAM bytes per launch: measured at this size where a
+        # one-pass capture exists, else the norb-12 full capture's ratio to
+        # the algorithmic bytes (psi's digit words read once, G written
+        # once) scaled to this workload
+        meas = FUSED_TRAFFIC_MEASURED.get(NORB) if NALPHA == NBETA == NORB // 2 else None
+        if meas:
+            traffic = meas[0] + meas[1]
+            traffic_src = (f"ncu one-pass capture at norb {NORB}: dram read {meas[0] / 1e9:.2f} GB"
+                           f" + write {meas[1] / 1e9:.2f} GB")
+        else:
+            traffic = FUSED_TRAFFIC_RATIO * (24.0 * n + 16.0 * P * n)
+            traffic_src = "ncu capture at norb 12 scaled by algorithmic bytes"
     roofline = {"kernel": names[dom], "bound": dk["bound"],
                 "achieved": dk["achieved"], "peak": dk["peak"],
                 "unit": dk["unit"],
                 "frac": (dk["achieved"] / dk["peak"]) if dk["achieved"] else None,
                 "traffic": traffic,
-                "traffic_source": "ncu capture at norb 12 scaled by algorithmic bytes"
-                if traffic else None,
+                "traffic_source": traffic_src,
                 "peak_source": peak_src if dk["bound"] != "fp64"
                 else "torch float64 matmul 4096^3 on a GB300"}
     # whole-apply HBM view with the uncompressed dvec byte model 16 norb^2 + 32
