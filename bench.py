@@ -31,6 +31,8 @@ same line (default sector norb=12 (6a,6b); --davidson-norb, --no-davidson).
                                  Davidson to 1e-6 at norb 16, learned vs plain
   python bench.py --diag         the norb-14 diagonal-Coulomb evolve, 20 calls
   python bench.py --rdm          the norb-14 one- and two-particle RDMs
+  python bench.py --rows         spin-orbital apply (norb 12), orbital rotation
+                                 and save/read (norb 14)
 """
 
 import argparse
@@ -657,6 +659,92 @@ def rdm_leg(norb=14):
             "rdm12_fp64_tflops": 8.0 * p * (p + 1) / 2 * n / (t12 / 1e3) / 1e12}
 
 
+def rows_leg():
+    """The rows either side of the apply, timed once each after a warm-up
+    (CUDA events / wall clock): the spin-orbital two-body apply
+    (FqeData.apply with 2 norb spin orbitals) at norb 12 (6a,6b) on the
+    tensor cores and in FP64, with their relative difference; the orbital
+    rotation Wavefunction.transform of the norb-14 (7a,7b) sector under a
+    seeded random unitary (2 norb column passes); and save + read of that
+    wavefunction through a temporary file."""
+    import numpy
+    import torch
+    import fqe_gb300
+    from fqe_gb300 import settings, synthetic
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        r = fn()
+        e.record()
+        torch.cuda.synchronize()
+        return r, s.elapsed_time(e)
+
+    out = {}
+    old = settings.precision
+    try:
+        norb, na, nb = 12, 6, 6
+        rng = numpy.random.default_rng(SEED + 12)
+        h1s, h2s, psi = synthetic.sector(norb, na, nb, synthetic.default_nchol(norb), SEED)
+        # spin-orbital integrals: the spatial ones in both spin blocks plus an
+        # alpha-beta asymmetry, so the operator is not spin-free
+        n2 = 2 * norb
+        h1 = numpy.zeros((n2, n2))
+        h1[:norb, :norb] = h1s
+        h1[norb:, norb:] = h1s + 0.01 * numpy.diag(rng.normal(size=norb))
+        h2 = numpy.zeros((n2,) * 4)
+        for sa in (0, norb):
+            for sb in (0, norb):
+                h2[sa:sa + norb, sb:sb + norb, sa:sa + norb, sb:sb + norb] = h2s
+        d = fqe_gb300.FqeData(na, nb, norb)
+        d.set_wfn(strategy="from_data", raw_data=psi)
+        res = {}
+        row = {}
+        for prec in ("ozaki", "fp64"):
+            settings.precision = prec
+            d.apply((h1, h2))
+            r, ms = timed(lambda: d.apply((h1, h2)))
+            res[prec] = r.coeff.clone()
+            row[f"{prec}_ms"] = ms
+        row["rel_diff_ozaki_vs_fp64"] = float(torch.linalg.norm(res["ozaki"] - res["fp64"])
+                                              / torch.linalg.norm(res["fp64"]))
+        row["workload"] = (f"spin-orbital apply, norb={norb} ({na}a,{nb}b), "
+                           f"{psi.size} determinants, {2 * norb} spin orbitals")
+        out["spin_orbital_apply"] = row
+        del res, d
+        settings.precision = "fp64"
+        norb, na, nb = 14, 7, 7
+        key = (na + nb, 0)
+        _, _, psi = synthetic.sector(norb, na, nb, synthetic.default_nchol(norb), SEED)
+        w = fqe_gb300.Wavefunction([[na + nb, 0, norb]])
+        w.set_wfn(strategy="from_data", raw_data={key: psi})
+        a = rng.normal(size=(norb, norb)) + 1j * rng.normal(size=(norb, norb))
+        u, _ = numpy.linalg.qr(a)
+        w.transform(u)
+        _, ms = timed(lambda: w.transform(u))
+        out["orbital_rotation"] = {
+            "workload": f"Wavefunction.transform, norb={norb} ({na}a,{nb}b), "
+                        f"{psi.size} determinants, random unitary",
+            "ms": ms, "norm_after": float(torch.linalg.norm(w.get_coeff(key)))}
+        with tempfile.TemporaryDirectory() as tmp:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            w.save("wfn.pkl", tmp)
+            t1 = time.perf_counter()
+            w2 = fqe_gb300.Wavefunction([[na + nb, 0, norb]])
+            w2.read("wfn.pkl", tmp)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            same = bool(torch.equal(w2.get_coeff(key), w.get_coeff(key)))
+        out["save_read"] = {"workload": f"save + read, norb={norb}, {psi.size * 16} bytes",
+                            "save_s": t1 - t0, "read_s": t2 - t1, "identical": same}
+    finally:
+        settings.precision = old
+    return out
+
+
 def taylor_leg(norb=16, steps=20, dt=0.05, accuracy=1e-12, fp64_check=True):
     """The norb-16 (8a,8b) configuration: `steps` Taylor steps of dt on the
     tensor cores (Ozaki-split BF16), per step the wall time, the number of
@@ -847,6 +935,9 @@ def main():
     ap.add_argument("--taylor16", action="store_true",
                     help="only the norb-16 (8a,8b) 20-step Taylor evolution "
                          "(tensor cores) with the first step against FP64")
+    ap.add_argument("--rows", action="store_true",
+                    help="only the rows beside the apply: spin-orbital apply, "
+                         "orbital rotation, save/read")
     ap.add_argument("--rdm", action="store_true",
                     help="only the norb-14 one- and two-particle RDMs")
     ap.add_argument("--diag", action="store_true",
@@ -864,7 +955,7 @@ def main():
                      args.nchol or synthetic.default_nchol(args.norb))
     if args.impl == "reference":
         return run_reference(args)
-    if args.configs or args.taylor16 or args.batch or args.diag or args.rdm:
+    if args.configs or args.taylor16 or args.batch or args.diag or args.rdm or args.rows:
         import torch
         import fqe_gb300
         torch.cuda.set_device(0)
@@ -875,6 +966,8 @@ def main():
             print(json.dumps({"diag_coulomb": diag_leg()}), flush=True)
         elif args.rdm:
             print(json.dumps({"rdm": rdm_leg()}), flush=True)
+        elif args.rows:
+            print(json.dumps({"rows": rows_leg()}), flush=True)
         elif args.taylor16:
             print(json.dumps({"taylor_norb16": taylor_leg(
                 fp64_check=not args.no_fp64_check)}), flush=True)
