@@ -29,7 +29,9 @@ def _apply(gpu, norb, na, nb, h1, h2, psi):
 
 
 @pytest.mark.parametrize("norb,na,nb", [(4, 2, 2), (6, 3, 2), (8, 4, 4), (9, 4, 3),
-                                        (10, 5, 5), (11, 3, 6), (12, 6, 6), (13, 6, 5)])
+                                        (10, 5, 5), (11, 3, 6), (12, 6, 6), (13, 6, 5),
+                                        # an empty or full spin: one alpha or beta string
+                                        (9, 0, 4), (8, 8, 2), (7, 3, 0)])
 def test_ozaki_matches_fp64_and_oracle(ozaki, oracle, norb, na, nb):
     from fqe_gb300 import synthetic, settings
     h1, h2, rng = synthetic.integrals(norb, norb + 4, 100 + norb)
@@ -122,7 +124,7 @@ def test_plans_of_different_sizes_coexist(gpu, ozaki):
 @pytest.mark.parametrize("norb,na,nb,limit", [
     (10, 5, 5, 40 << 20),     # beta-column blocks of 64 columns
     (10, 5, 4, 7 << 20),      # blocks of 32 columns (the narrowest)
-    (17, 2, 2, None),         # P = 153: two passes of output pairs, 3-group slicer
+    (17, 2, 2, None),         # P = 153: two passes of output pairs
     (17, 3, 2, 40 << 20)])    # both at once
 def test_blocks_and_passes(gpu, oracle, ozaki, norb, na, nb, limit):
     from fqe_gb300 import _lib, synthetic
