@@ -125,20 +125,22 @@ __device__ __forceinline__ double2 dvec_value(int64_t p, int64_t lena, int64_t l
                                               int64_t b, const int32_t* __restrict__ tabA,
                                               const int32_t* __restrict__ tabB,
                                               const double2* __restrict__ psi) {
+  // signs applied by flipping the sign bit (integer XOR), not by FP64
+  // multiplies: the Gram kernel that calls this is FP64-bound
   double vx = 0.0, vy = 0.0;
   const int32_t ca = tabA[p * lena + a];
   if (ca) {
     const double2 x = psi[(int64_t)(abs(ca) - 1) * lenb + b];
-    const double s = ca > 0 ? 1.0 : -1.0;
-    vx = s * x.x;
-    vy = s * x.y;
+    const unsigned long long sb = ca < 0 ? 0x8000000000000000ull : 0ull;
+    vx = __longlong_as_double(__double_as_longlong(x.x) ^ sb);
+    vy = __longlong_as_double(__double_as_longlong(x.y) ^ sb);
   }
   const int32_t cb = tabB[p * lenb + b];
   if (cb) {
     const double2 x = psi[a * lenb + (abs(cb) - 1)];
-    const double s = cb > 0 ? 1.0 : -1.0;
-    vx += s * x.x;
-    vy += s * x.y;
+    const unsigned long long sb = cb < 0 ? 0x8000000000000000ull : 0ull;
+    vx += __longlong_as_double(__double_as_longlong(x.x) ^ sb);
+    vy += __longlong_as_double(__double_as_longlong(x.y) ^ sb);
   }
   return make_double2(vx, vy);
 }

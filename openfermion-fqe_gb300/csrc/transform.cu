@@ -41,7 +41,26 @@ struct ColumnCoefs {
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+
+// acc += (neg ? -m : m) * v in four FP64 FMAs: the sign is flipped in m's
+// bits (integer XOR), not by an FP64 multiply or subtraction (the column
+// steps are FP64-bound on GB300).
+__device__ __forceinline__ void signed_madd(double2& acc, double2 m, double2 v, bool neg) {
+  const unsigned long long sb = neg ? 0x8000000000000000ull : 0ull;
+  const double mx = __longlong_as_double(__double_as_longlong(m.x) ^ sb);
+  const double my = __longlong_as_double(__double_as_longlong(m.y) ^ sb);
+  acc.x = fma(mx, v.x, acc.x);
+  acc.x = fma(-my, v.y, acc.x);
+  acc.y = fma(mx, v.y, acc.y);
+  acc.y = fma(my, v.x, acc.y);
+}
 }  // namespace
+
+// The source lookups of a column step come in groups of kGroup: the group's
+// table entries are read first, then its source values, then they are
+// accumulated in orbital order (the order of the one-at-a-time loop, so the
+// sums are the same), which keeps kGroup loads in flight per thread.
+constexpr int kGroup = 8;
 
 // Alpha column step: one CTA per (target row T, block of beta columns).
 __global__ void __launch_bounds__(256) k_column_alpha(int norb, int icol, int64_t lena,
@@ -60,19 +79,20 @@ __global__ void __launch_bounds__(256) k_column_alpha(int norb, int icol, int64_
     return;
   }
   double2 acc = x;
-  for (int i = 0; i < norb; ++i) {
-    if (i == icol) continue;
-    const int32_t c = tab[(int64_t)(i * norb + icol) * lena + T];  // uniform in the CTA
-    if (!c) continue;
-    const double2 v = in[(int64_t)(abs(c) - 1) * lenb + b];
-    const double2 p = cmul(cf.m[i], v);
-    if (c > 0) {
-      acc.x += p.x;
-      acc.y += p.y;
-    } else {
-      acc.x -= p.x;
-      acc.y -= p.y;
+  for (int i0 = 0; i0 < norb; i0 += kGroup) {
+    int32_t c[kGroup];
+    double2 v[kGroup];
+#pragma unroll
+    for (int u = 0; u < kGroup; ++u) {  // uniform in the CTA
+      const int i = i0 + u;
+      c[u] = (i < norb && i != icol) ? tab[(int64_t)(i * norb + icol) * lena + T] : 0;
     }
+#pragma unroll
+    for (int u = 0; u < kGroup; ++u)
+      v[u] = c[u] ? in[(int64_t)(abs(c[u]) - 1) * lenb + b] : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int u = 0; u < kGroup; ++u)
+      if (c[u]) signed_madd(acc, cf.m[i0 + u], v[u], c[u] < 0);
   }
   out[T * lenb + b] = acc;
 }
@@ -94,18 +114,20 @@ __global__ void __launch_bounds__(256) k_column_beta(int norb, int icol, int64_t
     return;
   }
   double2 acc = x;
-  for (int i = 0; i < norb; ++i) {
-    if (i == icol) continue;
-    const int32_t c = tab[(int64_t)(i * norb + icol) * lenb + T];
-    if (!c) continue;
-    const double2 p = cmul(cf.m[i], row[abs(c) - 1]);
-    if (c > 0) {
-      acc.x += p.x;
-      acc.y += p.y;
-    } else {
-      acc.x -= p.x;
-      acc.y -= p.y;
+  for (int i0 = 0; i0 < norb; i0 += kGroup) {
+    int32_t c[kGroup];
+    double2 v[kGroup];
+#pragma unroll
+    for (int u = 0; u < kGroup; ++u) {
+      const int i = i0 + u;
+      c[u] = (i < norb && i != icol) ? tab[(int64_t)(i * norb + icol) * lenb + T] : 0;
     }
+#pragma unroll
+    for (int u = 0; u < kGroup; ++u)
+      v[u] = c[u] ? row[abs(c[u]) - 1] : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int u = 0; u < kGroup; ++u)
+      if (c[u]) signed_madd(acc, cf.m[i0 + u], v[u], c[u] < 0);
   }
   out[a * lenb + T] = acc;
 }
