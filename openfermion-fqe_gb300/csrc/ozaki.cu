@@ -661,15 +661,48 @@ __global__ void k_oz_globalexp(int64_t lena, const int32_t* __restrict__ rowexp,
 // digit b (b = 1..5) = floor(r / 2^k + 1/2) with k = 8 (6 - b) and r the
 // remainder so far (|r| <= 128 2^k, so the digit lies in [-128, 128]); the
 // last digit is the final remainder.  Returned as floats digit * 2^-8b.
+// A small integer (|d| < 2^22) as a float, exactly, without a conversion
+// instruction: the bits of 1.5 * 2^23 + d, minus 1.5 * 2^23.
+__device__ __forceinline__ float small_int_float(int d) {
+  return __int_as_float(0x4B400000 + d) - 12582912.0f;
+}
+
 __device__ __forceinline__ void psi_digits(long long x, float (&f)[kDSlices]) {
 #pragma unroll
   for (int b = 1; b < kDSlices; ++b) {
     const int k = 8 * (kDSlices - b);
-    const long long dgt = (x + (1ll << (k - 1))) >> k;
+    const long long dgt = (x + (1ll << (k - 1))) >> k;  // in [-128, 128]
     x -= dgt << k;
-    f[b - 1] = (float)dgt * __int_as_float((127 - 8 * b) << 23);
+    f[b - 1] = small_int_float((int)dgt) * __int_as_float((127 - 8 * b) << 23);
   }
-  f[kDSlices - 1] = (float)x * __int_as_float((127 - 8 * kDSlices) << 23);
+  f[kDSlices - 1] = small_int_float((int)x) * __int_as_float((127 - 8 * kDSlices) << 23);
+}
+
+// v * 2^e rounded to the nearest integer, ties to even, built from the bits
+// of v with integer operations only (GB300 runs FP64 multiplies and double
+// conversions at a small fraction of its integer rate).  The caller keeps
+// |v| < 2^(47 - e), so the result is below 2^47; v is finite.
+__device__ __forceinline__ long long fixed_rn(double v, int e) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int be = (int)((bits >> 52) & 0x7FF);
+  unsigned long long m = bits & 0xFFFFFFFFFFFFFull;
+  int s = e - 1074;  // subnormal: m * 2^-1074
+  if (be) {
+    m |= 1ull << 52;
+    s = e + be - 1075;
+  }
+  unsigned long long q;
+  if (s >= 0) {
+    q = m << s;
+  } else if (s <= -64) {
+    q = 0;
+  } else {
+    const int r = -s;
+    q = m >> r;
+    const unsigned long long rem = m & ((1ull << r) - 1ull), half = 1ull << (r - 1);
+    if (rem > half || (rem == half && (q & 1ull))) ++q;
+  }
+  return (bits >> 63) ? -(long long)q : (long long)q;
 }
 
 // The digit planes of psi at the global exponent g0: pdA[i] = digits 1-4,
@@ -679,17 +712,15 @@ __global__ void k_oz_digits(int64_t n, const double2* __restrict__ psi,
                             uint2* __restrict__ pdB) {
   const int g0 = misc[0];
   const bool skip = misc[2] != 0;  // non-finite input: the output is NaN anyway
-  // 2^(47 - g0) in two factors, each within double range for any finite psi
-  const int e = 47 - g0, e1 = e / 2, e2 = e - e1;
-  const double s1 = __longlong_as_double((long long)(1023 + e1) << 52);
-  const double s2 = __longlong_as_double((long long)(1023 + e2) << 52);
+  // psi * 2^(47 - g0), |psi| < 2^g0, as 47-bit fixed point
+  const int e = 47 - g0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     float fr[kDSlices] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, fi[kDSlices] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (!skip) {
       const double2 v = psi[i];
-      psi_digits(__double2ll_rn((v.x * s1) * s2), fr);
-      psi_digits(__double2ll_rn((v.y * s1) * s2), fi);
+      psi_digits(fixed_rn(v.x, e), fr);
+      psi_digits(fixed_rn(v.y, e), fi);
     }
     uint32_t wd[kDSlices];
 #pragma unroll
