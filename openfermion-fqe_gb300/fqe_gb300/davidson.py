@@ -203,10 +203,19 @@ def davidson(hamiltonian: RestrictedHamiltonian, nalpha: int, nbeta: int,
     AV: List[torch.Tensor] = []
 
     def orthonormal_add(t: torch.Tensor) -> bool:
-        for _ in range(2):  # block classical Gram-Schmidt, twice
-            if V:
-                _block_axpy(-_block_vdot(V, t), V, t)
+        # block classical Gram-Schmidt with the Daniel-Gragg-Kaufman-Stewart
+        # test: a second pass only when the first removed more than
+        # 1 - 1/sqrt(2) of the norm (then the result is orthogonal to working
+        # precision either way); each pass is FP64-bound on GB300
         nrm = _norm(t)
+        for _ in range(2):
+            if not V:
+                break
+            before = nrm
+            _block_axpy(-_block_vdot(V, t), V, t)
+            nrm = _norm(t)
+            if nrm >= 0.7071067811865476 * before:
+                break
         if nrm < 1.0e-10:
             return False
         _scale(1.0 / nrm, t)
