@@ -63,13 +63,13 @@ def set_workload(norb, nalpha, nbeta, nchol):
 UNIT = "det/s"
 # the tensor-core contraction: BF16 slices of D (psi's digits) and products
 OZ_DSLICES, OZ_PRODUCTS = 6, 20
-# DRAM bytes of one k_oz_fused launch over its algorithmic bytes, from the
-# norb-12 ncu capture (profiles/k_oz_fused_norb12.md: psi's digit planes fit
-# in L2 there), used for sizes without a capture of their own
+# DRAM bytes of one k_oz_fused launch over its algorithmic bytes, from a full
+# ncu capture of the norb-12 bench command (psi's digit planes fit in L2
+# there), used for sizes without a capture of their own
 FUSED_TRAFFIC_RATIO = 1.03
 # measured DRAM bytes (read, write) of one k_oz_fused launch by norb for the
-# half-filled sector, one-pass ncu captures of the bench command itself
-# (profiles/k_oz_fused_norb14_dram.md)
+# half-filled sector: one-pass ncu counters (dram__bytes_read.sum,
+# dram__bytes_write.sum) on the bench command itself
 FUSED_TRAFFIC_MEASURED = {14: (13.69e9, 19.74e9)}
 
 
