@@ -15,7 +15,7 @@
 // at most two psi entries with signs +-1 (one alpha source, one beta source:
 // every target string has at most one source under each pair operator), so
 // D's digit b is the signed sum of its sources' digits b, in [-256, 256]:
-// exact in BF16.  The slicer therefore only gathers digits and adds them (no
+// exact in BF16.  The producers therefore only gather digits and add them (no
 // rounding, no per-determinant exponent).  Slices are stored as their true
 // values (digit * 2^{-8b}), so every product lands on one absolute scale and
 // the products are grouped by level L = a + b into four TMEM accumulators:

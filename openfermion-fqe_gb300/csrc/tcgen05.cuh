@@ -162,29 +162,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
 
 namespace fqegpu {
 namespace tc {
-// Arrive once on `bar` and add `bytes` to its expected transaction count.
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile(
-      "{\n\t.reg .b64 st;\n\t"
-      "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)),
-      "r"(bytes)
-      : "memory");
-}
-
-// Bulk (non-tensor) copy global -> shared, completing `bytes` transactions on
-// `bar`.  Both addresses 16-byte aligned, bytes a multiple of 16.
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
-                                         uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-}  // namespace tc
-}  // namespace fqegpu
-
-namespace fqegpu {
-namespace tc {
 // tcgen05.ld of 32 lanes x 4 columns without the wait: several loads can be
 // in flight; tmem_wait_ld_tied() waits for all of them.
 __device__ __forceinline__ void tmem_ld4_nowait(uint32_t taddr, uint32_t (&r)[4]) {

@@ -5,7 +5,7 @@ contraction G = V D of this project's apply, for checking its numerical
 design on the CPU.  The reference has no counterpart: it contracts in FP64
 (lib/fqe_data.c:879-970); the FP64 result here is the exact reference value.
 
-What is modelled (csrc/ozaki.cu, k_oz_digits / k_oz_slice / k_oz_mma):
+What is modelled (csrc/ozaki.cu, k_oz_digits and k_oz_fused):
 
 * each row of V is scaled by its exponent e (max |V| < 2^e), rounded to a
   40-bit magnitude and cut into five bytes; slice a holds
@@ -19,7 +19,8 @@ What is modelled (csrc/ozaki.cu, k_oz_digits / k_oz_slice / k_oz_mma):
   3, 4 alone (integer sums below 2^24 at one scale: exact) and levels 5..7
   together;
 * the four level sums are combined by a chain of exact two-sums (no level
-  is assumed to hold the leading bits) and scaled by 2^(e_row + g0 + 1).
+  is assumed to hold the leading bits) into an unnormalised FP32 pair and
+  scaled by 2^(e_row + g0 + 1).
 
 `contract` models the form the kernel had before: D's columns scaled by
 their exact exponents and rounded to 40-bit magnitudes (five slices, 19
@@ -144,7 +145,7 @@ def contract(V, D, e_det=None):
 
 
 # ---- the gather-free slicing: psi cut once into digits -----------------------
-# csrc/ozaki.cu, k_oz_digits / k_oz_slice: psi is scaled by one global
+# csrc/ozaki.cu, k_oz_digits / k_oz_fused: psi is scaled by one global
 # exponent g0 (max |Re|, |Im| < 2^g0) to a 47-bit fixed-point integer and cut
 # into six balanced base-256 digits in [-128, 128] (the last digit exact),
 # stored as digit * 2^-8b; a D entry is a sum of at most two psi entries with
