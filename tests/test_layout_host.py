@@ -71,3 +71,23 @@ def test_producer_pairs_and_bank_phases(pw):
     for phase in range(4):
         groups = {(off // 16) % 8 for _, _, off in lanes[8 * phase: 8 * phase + 8]}
         assert len(groups) == 8
+
+
+@pytest.mark.parametrize("NP", [16, 80, 112, 128])
+def test_epilogue_stores_every_output_once(NP):
+    """Epilogue warps w < 8 of k_oz_fused: TMEM lane quarter w & 3, column
+    half w >> 2 (NP / 2 pairs each); TMEM lane = MMA row = 64 * half + 2 det
+    + part.  Over one tile pair every (tile half, determinant, part, pair) is
+    stored exactly once."""
+    cw = NP // 2
+    seen = set()
+    for w in range(8):
+        quarter, cg = w & 3, w >> 2
+        for lane in range(32):
+            row = 32 * quarter + lane
+            half, det, part = row >> 6, (row & 63) >> 1, row & 1
+            for c in range(cw):
+                key = (half, det, part, cg * cw + c)
+                assert key not in seen
+                seen.add(key)
+    assert len(seen) == 2 * 32 * 2 * NP
